@@ -1,0 +1,345 @@
+"""Benchmark: Fock builds/s of the GPU direct-SCF J/K build.
+
+Workload (N=1): seeded (H2O)_8 water cluster, 6-31G* (Cartesian d), 152 AOs,
+80 shells; Schwarz cutoff 1e-12; FP32 cutoff 1e-5 for the mixed path.  The
+density is the converged FP64 RHF density of that cluster (computed once,
+outside the timed region).  One step = one Fock build J, K = jk(D) (the two
+einsums of the reference's hf.py:300 without the N^4 tensor), mixed precision.
+
+Reported:
+* value        Fock builds/s, mixed path, D/J/K resident in HBM; L2 flushed
+               (256 MB write) before every step, each step timed by CUDA events
+* e2e          same metric through the public API with host buffers: pinned D
+               -> device, Fock build, J and K -> pinned host, every step
+* fp64         the all-FP64 build, same protocol (the plain FP64 GPU baseline)
+* roofline     dominant class kernel: algorithmic FLOPs / its event time vs the
+               FMA peak of its precision measured live by an FMA-chain kernel
+* cpu_baseline the oracle's restatement of the reference algorithm (one call
+               per unique AO quartet, 5 Rys roots, no screening, OpenMP over
+               all host cores) on a bounded stride sample, extrapolated
+* clocks       nvidia-smi samples taken during the timed region
+
+``--impl reference`` times the reference's CPU algorithm (oracle port, all host
+cores) on the same workload and prints the same metric.
+Multi-GPU (torchrun, N ranks): replicas -- every rank builds the same Fock
+matrix; value = sum over ranks of builds / max-over-ranks time (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "Fock builds/s ((H2O)8 6-31G*, mixed FP32/FP64, Schwarz 1e-12)"
+CUTOFF = 1e-12
+FP32_CUTOFF = 1e-5
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload(nwater=8, basis="6-31g*", seed=0):
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.molecule import Molecule
+    s, x = G.water_cluster(nwater, seed=seed)
+    return Molecule.from_geometry(s, x, basis)
+
+
+def cfg_dict(mol, nwater, basis):
+    return {"workload": "(H2O)%d water cluster, %s, seed 0" % (nwater, basis.upper()), "nao": mol.nao,
+            "nshell": len(mol.shells), "schwarz_cutoff": CUTOFF, "fp32_cutoff": FP32_CUTOFF,
+            "density": "converged FP64 RHF", "l2": "flushed before every step (256 MB write)",
+            "parallelism": "replicas"}
+
+
+# ----------------------------------------------------------------------------
+def clock_sampler_start(path):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(path, "w")
+        return subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                stdout=f, stderr=subprocess.DEVNULL), f
+    except Exception:
+        return None, None
+
+
+def clock_sampler_stop(proc, f, path, device_index=0):
+    if proc is None:
+        return None
+    proc.terminate()
+    try:
+        proc.wait(timeout=5)
+    except Exception:
+        proc.kill()
+    f.close()
+    sm, smax, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in open(path):
+        t = [v.strip() for v in line.split(",")]
+        if len(t) < 9 or t[0] != str(device_index):
+            continue
+        try:
+            sm.append(float(t[1]))
+            smax.append(float(t[2]))
+        except ValueError:
+            continue
+        for nm, v in zip(names, t[5:9]):
+            if v.lower() == "active":
+                reasons.add(nm)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+def fma_peaks(dev):
+    """Live FMA-throughput peaks (TFLOP/s) of the FP64 and FP32 CUDA-core pipes."""
+    import torch
+    from segfault_py_gb300 import _lib
+    import ctypes as C
+    L = _lib.lib()
+    out = {}
+    for prec, name in ((0, "fp64"), (1, "fp32")):
+        flops = C.c_double(0.0)
+        ms = C.c_float(0.0)
+        _lib.check(L.sf_fma_peak(prec, C.byref(flops), C.byref(ms), C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        out[name] = flops.value / (ms.value * 1e-3) / 1e12
+    return out
+
+
+def time_steps(fn, steps, warmup, flush, stream):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        fn()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.scf import scf_diis
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nwater, basis = args.nwater, args.basis
+    mol = workload(nwater, basis)
+    fb = FockBuilder(mol, device=dev, cutoff=CUTOFF, fp32_cutoff=FP32_CUTOFF, precision="mixed")
+    r = scf_diis(mol, tol=1e-9, fb=fb, device=dev)
+    D = r.D.contiguous()
+    H = r.H
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    J = torch.empty_like(D)
+    K = torch.empty_like(D)
+
+    # error of the mixed build against the FP64 build at the converged density
+    def energy(prec):
+        fb.jk(D, precision=prec, out=(J, K))
+        F = H + J - 0.5 * K
+        return float(0.5 * torch.sum(D * (H + F)))
+    e64, emx = energy("fp64"), energy("mixed")
+
+    # stats + per-launch profile of one build per precision
+    prof = {}
+    for prec in ("fp64", "mixed"):
+        fb.set_profiling(True)
+        fb.jk(D, precision=prec, out=(J, K), stats=True)
+        prof[prec] = (dict(fb.last_stats), fb.slice_info())
+        fb.set_profiling(False)
+    st_mx, slices_mx = prof["mixed"]
+    st_64, slices_64 = prof["fp64"]
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk_path = os.path.join(REPO, "gpurun_out", "bench_clocks_rank%d.csv" % rank)
+    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    proc, fh = clock_sampler_start(clk_path) if rank == 0 else (None, None)
+    t_mx = time_steps(lambda: fb.jk(D, precision="mixed", out=(J, K)), args.steps, args.warmup, flush, stream)
+    t_64 = time_steps(lambda: fb.jk(D, precision="fp64", out=(J, K)), args.steps, args.warmup, flush, stream)
+    # e2e through the public API with host buffers
+    Dh = D.cpu().pin_memory()
+    Jh = torch.empty_like(Dh).pin_memory()
+    Kh = torch.empty_like(Dh).pin_memory()
+    Dd = torch.empty_like(D)
+
+    def e2e_step():
+        Dd.copy_(Dh, non_blocking=True)
+        fb.jk(Dd, precision="mixed", out=(J, K))
+        Jh.copy_(J, non_blocking=True)
+        Kh.copy_(K, non_blocking=True)
+    t_e2e = time_steps(e2e_step, args.steps, args.warmup, flush, stream)
+    torch.cuda.synchronize()
+    clocks = clock_sampler_stop(proc, fh, clk_path) if rank == 0 else None
+    if world > 1:
+        dist.barrier()
+    ms_mx, ms_64, ms_e2e = float(np.sum(t_mx)), float(np.sum(t_64)), float(np.sum(t_e2e))
+    if world > 1:
+        tt = torch.tensor([ms_mx, ms_64, ms_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_mx, ms_64, ms_e2e = tt.tolist()
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    steps = args.steps
+    value = world * steps / (ms_mx * 1e-3)
+    peaks = fma_peaks(dev)
+    # roofline of the dominant class kernel of the mixed build
+    dom = max(slices_mx, key=lambda s: s["ms"])
+    dom_prec = "fp64" if dom["precision"] == 0 else "fp32"
+    achieved = dom["flop_alg"] / (dom["ms"] * 1e-3) / 1e12 if dom["ms"] > 0 else 0.0
+    total_ms_mx = sum(s["ms"] for s in slices_mx)
+    comb = (st_mx["flop_alg_fp64"] / (peaks["fp64"] * 1e12) + st_mx["flop_alg_fp32"] / (peaks["fp32"] * 1e12))
+    build_frac = comb / (float(np.mean(t_mx)) * 1e-3)
+    nn = mol.nao * mol.nao * 8
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(mol, args.cpu_seconds)
+    rec = {
+        "metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms_mx / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+fp64 (mixed; FP64 accumulation)", "data": "synthetic",
+        "config": cfg_dict(mol, nwater, basis),
+        "e2e": {"value": world * steps / (ms_e2e * 1e-3), "unit": "Fock builds/s",
+                "h2d_bytes_per_step": nn, "d2h_bytes_per_step": 2 * nn},
+        "fp64": {"value": world * steps / (ms_64 * 1e-3), "unit": "Fock builds/s", "ms_per_step": ms_64 / steps,
+                 "quartets_per_s": st_64["quartets_fp64"] * steps / (ms_64 * 1e-3),
+                 "flop_alg": st_64["flop_alg_fp64"]},
+        "mixed_speedup_vs_fp64": ms_64 / ms_mx,
+        "quartets_per_s": (st_mx["quartets_fp64"] + st_mx["quartets_fp32"]) * world * steps / (ms_mx * 1e-3),
+        "prim_quartets_per_s": (st_mx["prim_quartets_fp64"] + st_mx["prim_quartets_fp32"]) * world * steps
+                               / (ms_mx * 1e-3),
+        "quartets": {"fp64": st_mx["quartets_fp64"], "fp32": st_mx["quartets_fp32"],
+                     "unscreened": st_mx["quartets_total"]},
+        "energy_error_mixed_vs_fp64": emx - e64,
+        "gpu_launches": int(st_mx["launches"]) * steps * 2 + int(st_64["launches"]) * steps,
+        "roofline": {"bound": dom_prec, "achieved": achieved, "peak": peaks[dom_prec], "unit": "TFLOP/s",
+                     "frac": achieved / peaks[dom_prec] if peaks[dom_prec] else None, "traffic": None,
+                     "kernel": "jk_kernel<%d,%d,%d,%d,%s,T=%d>" % (dom["la"], dom["lb"], dom["lc"], dom["ld"],
+                                                                   dom_prec, dom["threads_per_quartet"]),
+                     "kernel_share": dom["ms"] / total_ms_mx if total_ms_mx else None,
+                     "peak_source": "live FMA-chain kernel (sf_fma_peak), this run",
+                     "build_combined_frac": build_frac},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(rec))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------
+def cpu_baseline(mol, seconds=15.0):
+    """Oracle port of the reference algorithm on a bounded stride sample of the
+    unique AO quartets (rows ij of the packed pair index with ij % stride == 0)."""
+    from oracle import oracle as O
+    n = mol.nao
+    cg = O.cgf_array(mol.cgfs)
+    D = np.eye(n) * 0.1
+    npair = n * (n + 1) // 2
+    tot = npair * (npair + 1) // 2
+    threads = os.cpu_count() or 1
+    stride = 4000
+    while True:
+        rows = np.arange(0, npair, stride)
+        cov = int(np.sum(rows + 1))
+        t = time.time()
+        O.jk_direct(cg, D, nthreads=threads, stride=stride, phase=0)
+        dt = time.time() - t
+        if dt * 3 > seconds or stride <= 1:
+            break
+        stride = max(1, int(stride * dt / seconds * 1.5) if dt > 0.05 else stride // 8)
+    full = dt * tot / cov
+    root = "reference root5 (transcribed)" if O.use_reference_root5(True) else "oracle root table"
+    O.use_reference_root5(False)
+    return {"value": 1.0 / full, "unit": "Fock builds/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d unique AO quartets (stride %d over packed pair rows), %.1f s, extrapolated"
+                      % (cov, tot, stride, dt),
+            "algorithm": "reference rys.eri_rys per AO quartet, 5 roots, no screening, direct J/K digestion",
+            "roots": root}
+
+
+def run_reference(args):
+    """The reference's CPU algorithm (oracle port) on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    mol = workload(args.nwater, args.basis)
+    n = mol.nao
+    cg = O.cgf_array(mol.cgfs)
+    D = np.eye(n) * 0.1
+    npair = n * (n + 1) // 2
+    tot = npair * (npair + 1) // 2
+    threads = os.cpu_count() or 1
+    use_ref = O.use_reference_root5(True)
+    stride = 40 if n > 100 else 1
+    rows = np.arange(0, npair, stride)
+    times = []
+    for i in range(args.warmup + args.steps):
+        phase = i % stride
+        rows = np.arange(phase, npair, stride)
+        cov = int(np.sum(rows + 1))
+        t = time.time()
+        O.jk_direct(cg, D, nthreads=threads, stride=stride, phase=phase)
+        dt = time.time() - t
+        if i >= args.warmup:
+            times.append(dt * tot / cov)
+    full = float(np.mean(times))
+    value = 1.0 / full
+    rec = {"metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": full * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "impl": "reference",
+           "config": cfg_dict(mol, args.nwater, args.basis),
+           "cpu_baseline": {"value": value, "unit": "Fock builds/s", "cores": threads, "kind": "port",
+                            "sample": "each step: 1/%d of the packed pair rows (unique AO quartets), extrapolated"
+                                      % stride,
+                            "roots": "reference root5 (transcribed)" if use_ref else "oracle root table"},
+           "e2e": {"value": value, "unit": "Fock builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(rec))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nwater", type=int, default=8)
+    ap.add_argument("--basis", default="6-31g*")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * segfock.h -- C ABI of libsegfock.so, the GB300 direct-SCF Fock builder.
+ *
+ * It replaces the ERI/Fock boundary of lyuhang428/SegFault_py (src/hf):
+ *
+ *   reference                                         here
+ *   --------------------------------------------------------------------------
+ *   rys.eri_rys(c1..c4, e1..e4, s1..s4, n1..n4,       sf_eri_batch: contracted
+ *     r1..r4) -> float, one Cartesian AO quartet        shell quartets, all
+ *     (src/hf/core/core.f90:967-1002, called at         Cartesian components
+ *     src/hf/hf.py:26-30 and :100-104)                  at once
+ *   build_eri_parallel: unique quartets i>=j, k>=l,   sf_fock_jk: the same
+ *     ij>=kl over Pool(8), dense N^4 tensor             unique (shell) quartets,
+ *     (src/hf/hf.py:33-61) + per-iteration J/K          Schwarz-screened, digested
+ *     einsums G = J - K/2 (src/hf/hf.py:300)            into J and K on the GPU
+ *   mmd2.overlap/kinetic/potential per AO pair        sf_one_electron
+ *     (src/hf/mmd2.py:14-84, hf.py:266-274)
+ *   Molecule/Atom/ContractedGaussianFunction          sf_create (shell table)
+ *     (src/hf/molecule.py:51-226)
+ *
+ * Conventions
+ *   - All compute entry points take DEVICE pointers and a cudaStream_t passed
+ *     as void* (NULL = legacy default stream).  Work is stream-ordered; the
+ *     host is not synchronised unless stated.
+ *   - AO order: shells in the order given, Cartesian components of a shell in
+ *     the reference order s; x,y,z; xx,xy,xz,yy,yz,zz (molecule.py:138-153).
+ *   - Matrices are row-major nao x nao doubles.
+ *   - Every function returns 0 on success or a negative SF_E* code; the text of
+ *     the last error of the calling thread is returned by sf_last_error().
+ *     Nothing traps or aborts on the device.
+ *   - Thread safety: one handle may be used by one host thread at a time.
+ */
+#ifndef SEGFOCK_H
+#define SEGFOCK_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SF_OK 0
+#define SF_EINVAL (-1)      /* bad argument                                  */
+#define SF_EUNSUPPORTED (-2)/* l > 2, contraction > SF_MAX_PRIM, ...        */
+#define SF_ECUDA (-3)       /* a CUDA runtime call failed                    */
+#define SF_ESTATE (-4)      /* call order (e.g. Fock build before Schwarz)   */
+#define SF_ENOMEM (-5)
+
+#define SF_MAX_L 2
+#define SF_MAX_PRIM 16
+
+/* precision modes of sf_fock_jk / sf_eri_batch */
+#define SF_PREC_FP64 0      /* every quartet in FP64                          */
+#define SF_PREC_FP32 1      /* every quartet in FP32 (FP64 accumulation)      */
+#define SF_PREC_MIXED 2     /* FP64 above the FP32 cutoff, FP32 below it      */
+
+typedef struct sf_handle sf_handle;
+
+/* One contracted Cartesian shell.  coefs are the contraction coefficients of
+ * the x^l component including its primitive normalisation; component
+ * (lx,ly,lz) is scaled by sqrt((2l-1)!! / ((2lx-1)!!(2ly-1)!!(2lz-1)!!)), so
+ * every Cartesian function is normalised individually as in
+ * src/hf/molecule.py:210-226. */
+typedef struct {
+    int32_t l;
+    int32_t nprim;
+    int32_t atom;
+    int32_t ao_offset;
+    double center[3];        /* bohr */
+    const double *exps;      /* host pointer, nprim values */
+    const double *coefs;     /* host pointer, nprim values */
+} sf_shell_desc;
+
+/* counters of the last sf_fock_jk call */
+typedef struct {
+    int64_t quartets_fp64;        /* canonical shell quartets done in FP64     */
+    int64_t quartets_fp32;        /* ... in FP32                               */
+    int64_t quartets_total;       /* canonical shell quartets before screening */
+    int64_t prim_quartets_fp64;
+    int64_t prim_quartets_fp32;
+    double flop_alg_fp64;         /* algorithmic FLOPs (Rys assembly + digestion) */
+    double flop_alg_fp32;
+    int32_t launches;             /* kernel launches issued by the call        */
+    int32_t reserved;
+} sf_stats;
+
+/* library version (major*10000 + minor*100 + patch) */
+int sf_version(void);
+
+/* text of the last error on this host thread ("" if none) */
+const char *sf_last_error(void);
+
+/* Build the shell table, primitive-pair data and Rys root tables on the
+ * current device.  Replaces Molecule/Atom/ContractedGaussianFunction set-up
+ * (src/hf/molecule.py:51-226).  Allocates device memory owned by the handle. */
+int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out);
+
+/* Same as sf_create (name used by earlier drafts of the interface). */
+int sf_build_shells(const sf_shell_desc *shells, int32_t nshell, sf_handle **out);
+
+void sf_destroy(sf_handle *h);
+
+/* number of Cartesian AOs and shell pairs of the handle */
+int32_t sf_nao(const sf_handle *h);
+int64_t sf_npairs(const sf_handle *h);
+
+/* Schwarz bounds Q_ab = sqrt(max |(ab|ab)|) for every shell pair a >= b,
+ * computed on the GPU in FP64 and kept in the handle (needed by sf_fock_jk).
+ * q_out (optional, host pointer, nshell*nshell doubles, symmetric) receives
+ * them.  Synchronises the stream.  The reference has no screening
+ * (hf.py:37-43 enumerates every quartet). */
+int sf_schwarz(sf_handle *h, double *q_out, void *stream);
+
+/* Coulomb and exchange matrices for a symmetric density D (device, nao*nao):
+ *   J_pq = sum_rs (pq|rs) D_rs,  K_pq = sum_rs (pr|qs) D_rs
+ * (the two einsums of src/hf/hf.py:300), over the canonical shell quartets
+ * with Q_ab Q_cd >= cutoff.  In SF_PREC_MIXED, quartets with
+ * Q_ab Q_cd < fp32_cutoff are evaluated in FP32; J and K are accumulated in
+ * FP64 in every mode.  J, K: device, nao*nao, overwritten.
+ * stats (optional, host) receives counters.  Does not synchronise unless
+ * stats is given. */
+int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t precision,
+               double cutoff, double fp32_cutoff, sf_stats *stats, void *stream);
+
+/* Restrict sf_fock_jk to the slice [part, part+1) of nparts equal-work slices
+ * of every quartet class (replica / multi-GPU partitioning hook; 0,1 = all). */
+int sf_set_partition(sf_handle *h, int32_t part, int32_t nparts);
+
+/* Raw contracted ERIs of nq shell quartets (device int32[nq*4] shell ids, any
+ * order of angular momenta).  out (device) receives, for quartet q at
+ * out_offsets[q] (device int64[nq]), the ncart(a)*ncart(b)*ncart(c)*ncart(d)
+ * integrals (ab|cd) in row-major component order.  precision: SF_PREC_FP64 or
+ * SF_PREC_FP32 (FP32 evaluation, stored as double). */
+int sf_eri_batch(sf_handle *h, const int32_t *quartets, int64_t nq, int32_t precision,
+                 double *out, const int64_t *out_offsets, void *stream);
+
+/* One-electron matrices (device, nao*nao each): overlap S, kinetic T and
+ * nuclear attraction V = sum_C -Z_C <a|1/r_C|b> for natom point charges
+ * (atom_xyz device [natom*3] bohr, charges device [natom]).
+ * src/hf/mmd2.py:14-84 with hf.py:266-274.  Any of S, T, V may be NULL. */
+int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges,
+                    int32_t natom, double *S, double *T, double *V, void *stream);
+
+/* Per-launch profiling of sf_fock_jk.  When on, every class kernel of a Fock
+ * build is bracketed by CUDA events on the caller's stream; sf_slice_info
+ * then reports, per launch ("slice" = one class in one precision), the work
+ * and the device time of the last profiled build (waits for its events).
+ * No counterpart in the reference (it only times whole SCF runs,
+ * src/hf/utils.py:76-83). */
+typedef struct {
+    int32_t cls;              /* canonical class id 0..20                      */
+    int32_t precision;        /* SF_PREC_FP64 or SF_PREC_FP32                 */
+    int32_t la, lb, lc, ld;
+    int64_t quartets;
+    int64_t prim_quartets;
+    double flop_alg;
+    float ms;                 /* device time of the last profiled launch      */
+    int32_t threads_per_quartet;
+} sf_slice_info;
+
+int sf_set_profiling(sf_handle *h, int32_t on);
+int32_t sf_slice_count(const sf_handle *h);
+int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out);
+
+/* FMA-throughput microbenchmark of the FP64 (precision 0) or FP32 (1)
+ * CUDA-core pipe on the current device: *flops executed in *ms.  It is the
+ * peak the roofline fractions are quoted against.  No counterpart in the
+ * reference.  Synchronises the stream. */
+int sf_fma_peak(int32_t precision, double *flops, float *ms, void *stream);
+
+/* Host evaluation of the library's Rys root table (for checks without a GPU):
+ * n-point rule at x, u[i] = t_i^2, w[i] weights; fp32 != 0 selects the
+ * single-precision table. */
+int sf_rys_roots_host(int32_t n, double x, int32_t fp32, double *u, double *w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SEGFOCK_H */

@@ -1,0 +1,21 @@
+"""GB300-native direct-SCF Fock builder (drop-in for the ERI/Fock path of
+lyuhang428/SegFault_py, src/hf).
+
+The compute path is libsegfock.so (sm_103a CUDA kernels behind a C ABI,
+include/segfock.h); this package is the Python host side: basis/molecule
+ingestion, the ctypes binding, the Fock builder and the SCF drivers.
+"""
+from .molecule import Atom, BasisSetNotAvailableError, ContractedGaussianFunction, Molecule  # noqa: F401
+
+__all__ = ["Molecule", "Atom", "ContractedGaussianFunction", "BasisSetNotAvailableError",
+           "FockBuilder", "eri_rys", "scf", "scf_damping", "scf_diis"]
+
+
+def __getattr__(name):
+    if name in ("FockBuilder", "eri_rys"):
+        from . import fock
+        return getattr(fock, name)
+    if name in ("scf", "scf_damping", "scf_diis", "SCFResult"):
+        from . import scf as _scf
+        return getattr(_scf, name)
+    raise AttributeError(name)

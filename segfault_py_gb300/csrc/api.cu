@@ -1,0 +1,664 @@
+// api.cu -- C ABI of libsegfock (declared in include/segfock.h) and the host
+// logic behind it: shell / pair tables, Schwarz ordering, the implicit
+// screened quartet lists and the launch sequence of one Fock build.
+//
+// Quartet enumeration.  The reference enumerates every unique AO quartet
+// i>=j, k>=l, ij>=kl (src/hf/hf.py:37-43).  Here the unit is the canonical
+// shell quartet: pairs (a,b) with l_a >= l_b (a >= b if equal), classes
+// (X|Y) with pair class X >= Y, and for X == Y the ket pair index <= the bra
+// pair index.  After sf_schwarz the pairs of each class are sorted by Q
+// descending, so for bra pair i the ket pairs that pass Q_i Q_j >= cutoff are
+// a prefix of the ket list; a quartet index q maps to (i, j) through the
+// prefix sums of those prefix lengths (no explicit quartet list is stored).
+// In the mixed mode the prefix splits at Q_i Q_j >= fp32_cutoff into an FP64
+// head and an FP32 tail.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "classes.h"
+#include "launch.h"
+#include "segfock.h"
+
+using namespace sf;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define SF_CK(call)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) return fail(SF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t m) {
+    if (m <= n && p) return cudaSuccess;
+    reset();
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(m, 1) * sizeof(T));
+    if (e == cudaSuccess) n = m;
+    return e;
+  }
+  cudaError_t upload(const std::vector<T> &v) {
+    cudaError_t e = alloc(v.size());
+    if (e != cudaSuccess) return e;
+    if (v.empty()) return cudaSuccess;
+    return cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+
+struct HostTables {
+  std::vector<double> t64;
+  std::vector<float> t32;
+  RysAsym asym;
+};
+
+const HostTables &host_tables() {
+  static HostTables T;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    T.t64.assign(rys_tab_size(kTabDeg64), 0.0);
+    T.t32.assign(rys_tab_size(kTabDeg32), 0.0f);
+    std::memset(&T.asym, 0, sizeof(T.asym));
+    rys_build_tables(T.t64.data(), T.t32.data(), &T.asym);
+  });
+  return T;
+}
+
+constexpr int kPairL[6][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {2, 2}};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+__global__ void symmetrize_kernel(const double *Jh, const double *Kh, double *J, double *K, int n) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * n) return;
+  const int i = (int)(idx / n), j = (int)(idx % n);
+  const int64_t t = (int64_t)j * n + i;
+  J[idx] = Jh[idx] + Jh[t];
+  K[idx] = Kh[idx] + Kh[t];
+}
+
+__global__ void to_float_kernel(const double *D, float *Df, int64_t n) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < n) Df[idx] = (float)D[idx];
+}
+
+}  // namespace
+
+struct sf_handle {
+  int device = 0;
+  int nshell = 0, nao = 0;
+  std::vector<int> l, nprim, atom, ao, spoff;
+  std::vector<double> cx, cy, cz, exps, coefs;
+  int cstart[kNumPairClass + 1] = {0};
+  std::vector<int> pa, pb, ppoff, pnp;
+  std::vector<double> pq;
+  std::vector<int> pairmap;   // a*nshell+b -> pair index (a,b canonical)
+  DBuf<int> d_l, d_nprim, d_ao, d_atom, d_spoff;
+  DBuf<double> d_cx, d_cy, d_cz, d_exps, d_coefs;
+  DBuf<int> d_pa, d_pb, d_ppoff, d_pnp;
+  DBuf<double> d_pq;
+  DBuf<double> d_pp64[6];
+  DBuf<float> d_pp32[6];
+  DBuf<double> d_tab64;
+  DBuf<float> d_tab32;
+  DBuf<double> d_Jh, d_Kh;
+  DBuf<float> d_D32;
+  DBuf<int> d_err;
+  bool have_schwarz = false;
+  // work cache
+  struct Slice {
+    int cls, prec;
+    ClassWork w;
+    int64_t quartets, prims;
+    double flops;
+  };
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev;   // 2 per slice while profiling
+  std::vector<Slice> slices;
+  DBuf<int64_t> d_prefix;
+  DBuf<int> d_jstart;
+  double c_cut = -1, c_cut32 = -1;
+  int c_prec = -1, c_part = -1, c_nparts = -1;
+  int64_t st_q[2] = {0, 0}, st_pq[2] = {0, 0}, st_total = 0;
+  double st_f[2] = {0, 0};
+  int part = 0, nparts = 1;
+  KParams kp;
+};
+
+namespace {
+
+void fill_kparams(sf_handle *h) {
+  KParams &k = h->kp;
+  k.sh = DevShells{h->d_l.p, h->d_nprim.p, h->d_ao.p, h->d_atom.p, h->d_cx.p, h->d_cy.p, h->d_cz.p};
+  k.pr = DevPairs{h->d_pa.p, h->d_pb.p, h->d_ppoff.p, h->d_pnp.p, h->d_pq.p};
+  k.p64 = DevPrims<double>{h->d_pp64[0].p, h->d_pp64[1].p, h->d_pp64[2].p, h->d_pp64[3].p, h->d_pp64[4].p,
+                           h->d_pp64[5].p};
+  k.p32 = DevPrims<float>{h->d_pp32[0].p, h->d_pp32[1].p, h->d_pp32[2].p, h->d_pp32[3].p, h->d_pp32[4].p,
+                          h->d_pp32[5].p};
+  k.tab64 = h->d_tab64.p;
+  k.tab32 = h->d_tab32.p;
+  k.asym = host_tables().asym;
+  k.nao = h->nao;
+  k.err = h->d_err.p;
+}
+
+int upload_pairs(sf_handle *h) {
+  SF_CK(h->d_pa.upload(h->pa));
+  SF_CK(h->d_pb.upload(h->pb));
+  SF_CK(h->d_ppoff.upload(h->ppoff));
+  SF_CK(h->d_pnp.upload(h->pnp));
+  SF_CK(h->d_pq.upload(h->pq));
+  h->pairmap.assign((size_t)h->nshell * h->nshell, -1);
+  for (size_t i = 0; i < h->pa.size(); ++i) h->pairmap[(size_t)h->pa[i] * h->nshell + h->pb[i]] = (int)i;
+  fill_kparams(h);
+  return SF_OK;
+}
+
+// number of leading ket pairs j (Q sorted descending) with qi * Q_j >= cut
+int64_t count_pass(const double *qy, int ny, double qi, double cut) {
+  const double *e = std::partition_point(qy, qy + ny, [&](double qj) { return qi * qj >= cut; });
+  return e - qy;
+}
+
+int build_work(sf_handle *h, int prec, double cut, double cut32) {
+  if (h->c_prec == prec && h->c_cut == cut && h->c_cut32 == cut32 && h->c_part == h->part &&
+      h->c_nparts == h->nparts)
+    return SF_OK;
+  h->slices.clear();
+  std::vector<int64_t> prefix;
+  std::vector<int> jstart;
+  struct Pending {
+    int cls, prec;
+    size_t poff, joff;
+    int64_t total, prims;
+    double flops;
+    int nX, x0, y0, same;
+  };
+  std::vector<Pending> pend;
+  h->st_q[0] = h->st_q[1] = h->st_pq[0] = h->st_pq[1] = 0;
+  h->st_f[0] = h->st_f[1] = 0.0;
+  h->st_total = 0;
+  for (int cls = 0; cls < kNumClass; ++cls) {
+    const ClassInfo &ci = kClassInfo[cls];
+    const int X = pair_class_of(ci.la, ci.lb), Y = pair_class_of(ci.lc, ci.ld);
+    const int x0 = h->cstart[X], y0 = h->cstart[Y];
+    const int nX = h->cstart[X + 1] - x0, nY = h->cstart[Y + 1] - y0;
+    const int same = X == Y;
+    h->st_total += same ? (int64_t)nX * (nX + 1) / 2 : (int64_t)nX * nY;
+    if (nX == 0 || nY == 0) continue;
+    const double *qx = h->pq.data() + x0, *qy = h->pq.data() + y0;
+    std::vector<int64_t> npy(nY + 1, 0);   // prefix of ket primitive-pair counts
+    for (int j = 0; j < nY; ++j) npy[j + 1] = npy[j] + h->pnp[y0 + j];
+    std::vector<int64_t> m(nX), m64(nX);
+    for (int i = 0; i < nX; ++i) {
+      int64_t mi = count_pass(qy, nY, qx[i], cut);
+      if (same) mi = std::min<int64_t>(mi, i + 1);
+      int64_t m6;
+      if (prec == SF_PREC_FP64) m6 = mi;
+      else if (prec == SF_PREC_FP32) m6 = 0;
+      else m6 = std::min<int64_t>(mi, count_pass(qy, nY, qx[i], std::max(cut32, cut)));
+      m[i] = mi;
+      m64[i] = m6;
+    }
+    const int nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
+    const double nabcd = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
+    for (int pr = 0; pr < 2; ++pr) {
+      Pending p;
+      p.cls = cls;
+      p.prec = pr;
+      p.poff = prefix.size();
+      p.joff = jstart.size();
+      p.nX = nX;
+      p.x0 = x0;
+      p.y0 = y0;
+      p.same = same;
+      int64_t run = 0, prims = 0;
+      prefix.push_back(0);
+      for (int i = 0; i < nX; ++i) {
+        const int64_t lo = pr == 0 ? 0 : m64[i], hi = pr == 0 ? m64[i] : m[i];
+        run += hi - lo;
+        prefix.push_back(run);
+        jstart.push_back((int)lo);
+        prims += (int64_t)h->pnp[x0 + i] * (npy[hi] - npy[lo]);
+      }
+      p.total = run;
+      p.prims = prims;
+      p.flops = (double)prims * nr * 4.0 * nabcd + 12.0 * nabcd * (double)run;
+      h->st_q[pr] += run;
+      h->st_pq[pr] += prims;
+      h->st_f[pr] += (double)prims * nr * 4.0 * nabcd + 12.0 * nabcd * (double)run;
+      if (run > 0) pend.push_back(p);
+      else {
+        prefix.resize(p.poff);
+        jstart.resize(p.joff);
+      }
+    }
+  }
+  SF_CK(h->d_prefix.upload(prefix));
+  SF_CK(h->d_jstart.upload(jstart));
+  for (const Pending &p : pend) {
+    ClassWork w;
+    w.prefix = h->d_prefix.p + p.poff;
+    w.jstart = h->d_jstart.p + p.joff;
+    w.nX = p.nX;
+    w.x0 = p.x0;
+    w.y0 = p.y0;
+    w.same = p.same;
+    w.q_begin = p.total * h->part / h->nparts;
+    w.q_end = p.total * (h->part + 1) / h->nparts;
+    if (w.q_end > w.q_begin) {
+      const double frac = (double)(w.q_end - w.q_begin) / (double)p.total;
+      h->slices.push_back({p.cls, p.prec, w, w.q_end - w.q_begin, (int64_t)(p.prims * frac), p.flops * frac});
+    }
+  }
+  h->c_prec = prec;
+  h->c_cut = cut;
+  h->c_cut32 = cut32;
+  h->c_part = h->part;
+  h->c_nparts = h->nparts;
+  return SF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sf_version(void) { return 100; }
+
+const char *sf_last_error(void) { return g_err.c_str(); }
+
+int32_t sf_nao(const sf_handle *h) { return h ? h->nao : -1; }
+
+int64_t sf_npairs(const sf_handle *h) { return h ? (int64_t)h->pa.size() : -1; }
+
+int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
+  if (!out) return fail(SF_EINVAL, "sf_create: out is NULL");
+  *out = nullptr;
+  if (!shells || nshell <= 0) return fail(SF_EINVAL, "sf_create: no shells");
+  for (int s = 0, ao = 0; s < nshell; ++s) {
+    const sf_shell_desc &d = shells[s];
+    if (d.l < 0 || d.l > SF_MAX_L) return fail(SF_EUNSUPPORTED, "sf_create: shell " + std::to_string(s) + " has l > 2");
+    if (d.nprim < 1 || d.nprim > SF_MAX_PRIM)
+      return fail(SF_EUNSUPPORTED, "sf_create: shell " + std::to_string(s) + " has an unsupported contraction length");
+    if (!d.exps || !d.coefs) return fail(SF_EINVAL, "sf_create: NULL primitive arrays");
+    if (d.ao_offset != ao) return fail(SF_EINVAL, "sf_create: ao_offset of shell " + std::to_string(s) + " is not contiguous");
+    for (int k = 0; k < d.nprim; ++k)
+      if (!(d.exps[k] > 0.0) || !std::isfinite(d.exps[k]) || !std::isfinite(d.coefs[k]))
+        return fail(SF_EINVAL, "sf_create: bad exponent/coefficient in shell " + std::to_string(s));
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(d.center[k])) return fail(SF_EINVAL, "sf_create: non-finite centre of shell " + std::to_string(s));
+    ao += ncart(d.l);
+  }
+  sf_handle *h = new sf_handle();
+  std::unique_ptr<sf_handle> guard(h);
+  SF_CK(cudaGetDevice(&h->device));
+  h->nshell = nshell;
+  h->spoff.push_back(0);
+  int nao = 0;
+  for (int s = 0; s < nshell; ++s) {
+    const sf_shell_desc &d = shells[s];
+    h->l.push_back(d.l);
+    h->nprim.push_back(d.nprim);
+    h->atom.push_back(d.atom);
+    h->ao.push_back(d.ao_offset);
+    h->cx.push_back(d.center[0]);
+    h->cy.push_back(d.center[1]);
+    h->cz.push_back(d.center[2]);
+    for (int k = 0; k < d.nprim; ++k) {
+      h->exps.push_back(d.exps[k]);
+      h->coefs.push_back(d.coefs[k]);
+    }
+    h->spoff.push_back((int)h->exps.size());
+    nao += ncart(d.l);
+  }
+  h->nao = nao;
+  // canonical shell pairs, grouped by pair class
+  const double kpre = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
+  std::vector<double> pp[6];
+  for (int pc = 0; pc < kNumPairClass; ++pc) {
+    h->cstart[pc] = (int)h->pa.size();
+    const int la = kPairL[pc][0], lb = kPairL[pc][1];
+    for (int a = 0; a < nshell; ++a) {
+      if (h->l[a] != la) continue;
+      for (int b = 0; b < nshell; ++b) {
+        if (h->l[b] != lb || (la == lb && b > a)) continue;
+        h->pa.push_back(a);
+        h->pb.push_back(b);
+        h->ppoff.push_back((int)pp[0].size());
+        h->pnp.push_back(h->nprim[a] * h->nprim[b]);
+        h->pq.push_back(0.0);
+        const double ABx = h->cx[a] - h->cx[b], ABy = h->cy[a] - h->cy[b], ABz = h->cz[a] - h->cz[b];
+        const double AB2 = ABx * ABx + ABy * ABy + ABz * ABz;
+        for (int i = h->spoff[a]; i < h->spoff[a + 1]; ++i)
+          for (int j = h->spoff[b]; j < h->spoff[b + 1]; ++j) {
+            const double al = h->exps[i], be = h->exps[j], p = al + be;
+            pp[0].push_back(p);
+            pp[1].push_back((al * h->cx[a] + be * h->cx[b]) / p);
+            pp[2].push_back((al * h->cy[a] + be * h->cy[b]) / p);
+            pp[3].push_back((al * h->cz[a] + be * h->cz[b]) / p);
+            pp[4].push_back(h->coefs[i] * h->coefs[j] * std::exp(-al * be / p * AB2) * kpre / p);
+            pp[5].push_back(0.5 / p);
+          }
+      }
+    }
+  }
+  h->cstart[kNumPairClass] = (int)h->pa.size();
+  for (int f = 0; f < 6; ++f) {
+    SF_CK(h->d_pp64[f].upload(pp[f]));
+    std::vector<float> v32(pp[f].begin(), pp[f].end());
+    SF_CK(h->d_pp32[f].upload(v32));
+  }
+  SF_CK(h->d_l.upload(h->l));
+  SF_CK(h->d_nprim.upload(h->nprim));
+  SF_CK(h->d_ao.upload(h->ao));
+  SF_CK(h->d_atom.upload(h->atom));
+  SF_CK(h->d_spoff.upload(h->spoff));
+  SF_CK(h->d_cx.upload(h->cx));
+  SF_CK(h->d_cy.upload(h->cy));
+  SF_CK(h->d_cz.upload(h->cz));
+  SF_CK(h->d_exps.upload(h->exps));
+  SF_CK(h->d_coefs.upload(h->coefs));
+  const HostTables &T = host_tables();
+  SF_CK(h->d_tab64.upload(T.t64));
+  SF_CK(h->d_tab32.upload(T.t32));
+  SF_CK(h->d_Jh.alloc((size_t)nao * nao));
+  SF_CK(h->d_Kh.alloc((size_t)nao * nao));
+  SF_CK(h->d_D32.alloc((size_t)nao * nao));
+  SF_CK(h->d_err.alloc(4));
+  SF_CK(cudaMemset(h->d_err.p, 0, 4 * sizeof(int)));
+  int rc = upload_pairs(h);
+  if (rc) return rc;
+  SF_CK(prepare_jk_f64());
+  SF_CK(prepare_jk_f32());
+  SF_CK(prepare_eri());
+  *out = guard.release();
+  g_err.clear();
+  return SF_OK;
+}
+
+int sf_build_shells(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
+  return sf_create(shells, nshell, out);
+}
+
+void sf_destroy(sf_handle *h) {
+  if (!h) return;
+  DeviceGuard g(h->device);
+  for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
+  delete h;
+}
+
+int sf_set_profiling(sf_handle *h, int32_t on) {
+  if (!h) return fail(SF_EINVAL, "sf_set_profiling: NULL handle");
+  h->profiling = on != 0;
+  return SF_OK;
+}
+
+int32_t sf_slice_count(const sf_handle *h) { return h ? (int32_t)h->slices.size() : -1; }
+
+int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out) {
+  if (!h || !out || idx < 0 || idx >= (int32_t)h->slices.size()) return fail(SF_EINVAL, "sf_get_slice_info: bad index");
+  DeviceGuard g(h->device);
+  const auto &s = h->slices[idx];
+  const ClassInfo &ci = kClassInfo[s.cls];
+  out->cls = s.cls;
+  out->precision = s.prec == 0 ? SF_PREC_FP64 : SF_PREC_FP32;
+  out->la = ci.la; out->lb = ci.lb; out->lc = ci.lc; out->ld = ci.ld;
+  out->quartets = s.quartets;
+  out->prim_quartets = s.prims;
+  out->flop_alg = s.flops;
+  out->threads_per_quartet = s.prec == 0 ? ci.t64 : ci.t32;
+  out->ms = -1.0f;
+  if (h->profiling && h->ev.size() >= 2 * h->slices.size()) {
+    SF_CK(cudaEventSynchronize(h->ev[2 * idx + 1]));
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, h->ev[2 * idx], h->ev[2 * idx + 1]) == cudaSuccess) out->ms = ms;
+    else cudaGetLastError();
+  }
+  return SF_OK;
+}
+
+int sf_schwarz(sf_handle *h, double *q_out, void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_schwarz: NULL handle");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  DBuf<double> dq;
+  const int np = (int)h->pa.size();
+  SF_CK(dq.alloc(np));
+  for (int pc = 0; pc < kNumPairClass; ++pc)
+    SF_CK(launch_schwarz(pc, h->kp, h->cstart[pc], h->cstart[pc + 1] - h->cstart[pc], dq.p, st));
+  std::vector<double> q(np);
+  SF_CK(cudaMemcpyAsync(q.data(), dq.p, np * sizeof(double), cudaMemcpyDeviceToHost, st));
+  SF_CK(cudaStreamSynchronize(st));
+  for (double v : q)
+    if (!std::isfinite(v)) return fail(SF_EINVAL, "sf_schwarz: non-finite Schwarz bound (bad basis data?)");
+  // sort every pair class by Q descending (stable)
+  for (int pc = 0; pc < kNumPairClass; ++pc) {
+    const int s0 = h->cstart[pc], s1 = h->cstart[pc + 1];
+    std::vector<int> idx(s1 - s0);
+    std::iota(idx.begin(), idx.end(), s0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return q[x] > q[y]; });
+    std::vector<int> a(idx.size()), b(idx.size()), po(idx.size()), n(idx.size());
+    std::vector<double> qq(idx.size());
+    for (size_t k = 0; k < idx.size(); ++k) {
+      a[k] = h->pa[idx[k]];
+      b[k] = h->pb[idx[k]];
+      po[k] = h->ppoff[idx[k]];
+      n[k] = h->pnp[idx[k]];
+      qq[k] = q[idx[k]];
+    }
+    std::copy(a.begin(), a.end(), h->pa.begin() + s0);
+    std::copy(b.begin(), b.end(), h->pb.begin() + s0);
+    std::copy(po.begin(), po.end(), h->ppoff.begin() + s0);
+    std::copy(n.begin(), n.end(), h->pnp.begin() + s0);
+    std::copy(qq.begin(), qq.end(), h->pq.begin() + s0);
+  }
+  int rc = upload_pairs(h);
+  if (rc) return rc;
+  h->have_schwarz = true;
+  h->c_prec = -1;   // invalidate quartet lists
+  if (q_out) {
+    std::fill(q_out, q_out + (size_t)h->nshell * h->nshell, 0.0);
+    for (int i = 0; i < np; ++i) {
+      q_out[(size_t)h->pa[i] * h->nshell + h->pb[i]] = h->pq[i];
+      q_out[(size_t)h->pb[i] * h->nshell + h->pa[i]] = h->pq[i];
+    }
+  }
+  g_err.clear();
+  return SF_OK;
+}
+
+int sf_set_partition(sf_handle *h, int32_t part, int32_t nparts) {
+  if (!h || nparts < 1 || part < 0 || part >= nparts) return fail(SF_EINVAL, "sf_set_partition: bad slice");
+  h->part = part;
+  h->nparts = nparts;
+  return SF_OK;
+}
+
+int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t precision, double cutoff,
+               double fp32_cutoff, sf_stats *stats, void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_fock_jk: NULL handle");
+  if (!D || !J || !K) return fail(SF_EINVAL, "sf_fock_jk: NULL matrix");
+  if (precision < SF_PREC_FP64 || precision > SF_PREC_MIXED) return fail(SF_EINVAL, "sf_fock_jk: bad precision");
+  if (!(cutoff >= 0.0) || !(fp32_cutoff >= 0.0)) return fail(SF_EINVAL, "sf_fock_jk: bad cutoff");
+  if (!h->have_schwarz) return fail(SF_ESTATE, "sf_fock_jk: call sf_schwarz first");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = build_work(h, precision, cutoff, fp32_cutoff);
+  if (rc) return rc;
+  const int n = h->nao;
+  const size_t nn = (size_t)n * n;
+  SF_CK(cudaMemsetAsync(h->d_Jh.p, 0, nn * sizeof(double), st));
+  SF_CK(cudaMemsetAsync(h->d_Kh.p, 0, nn * sizeof(double), st));
+  int launches = 0;
+  bool need32 = false;
+  for (const auto &s : h->slices) need32 |= s.prec == 1;
+  if (need32) {
+    to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, h->d_D32.p, (int64_t)nn);
+    SF_CK(cudaGetLastError());
+    ++launches;
+  }
+  if (h->profiling && h->ev.size() < 2 * h->slices.size()) {
+    while (h->ev.size() < 2 * h->slices.size()) {
+      cudaEvent_t e;
+      SF_CK(cudaEventCreate(&e));
+      h->ev.push_back(e);
+    }
+  }
+  for (size_t k = 0; k < h->slices.size(); ++k) {
+    const auto &s = h->slices[k];
+    if (h->profiling) SF_CK(cudaEventRecord(h->ev[2 * k], st));
+    if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, h->d_Jh.p, h->d_Kh.p, st));
+    else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st));
+    if (h->profiling) SF_CK(cudaEventRecord(h->ev[2 * k + 1], st));
+    ++launches;
+  }
+  symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(h->d_Jh.p, h->d_Kh.p, J, K, n);
+  SF_CK(cudaGetLastError());
+  ++launches;
+  if (stats) {
+    const double frac = 1.0 / h->nparts;
+    stats->quartets_fp64 = (int64_t)(h->st_q[0] * frac);
+    stats->quartets_fp32 = (int64_t)(h->st_q[1] * frac);
+    stats->quartets_total = h->st_total;
+    stats->prim_quartets_fp64 = (int64_t)(h->st_pq[0] * frac);
+    stats->prim_quartets_fp32 = (int64_t)(h->st_pq[1] * frac);
+    stats->flop_alg_fp64 = h->st_f[0] * frac;
+    stats->flop_alg_fp32 = h->st_f[1] * frac;
+    stats->launches = launches;
+    stats->reserved = 0;
+    SF_CK(cudaStreamSynchronize(st));
+  }
+  return SF_OK;
+}
+
+int sf_eri_batch(sf_handle *h, const int32_t *quartets, int64_t nq, int32_t precision, double *out,
+                 const int64_t *out_offsets, void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_eri_batch: NULL handle");
+  if (nq < 0 || (nq > 0 && (!quartets || !out || !out_offsets))) return fail(SF_EINVAL, "sf_eri_batch: bad arguments");
+  if (precision != SF_PREC_FP64 && precision != SF_PREC_FP32) return fail(SF_EINVAL, "sf_eri_batch: bad precision");
+  if (nq == 0) return SF_OK;
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<int32_t> hq((size_t)nq * 4);
+  std::vector<int64_t> hoff(nq);
+  SF_CK(cudaMemcpyAsync(hq.data(), quartets, hq.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  SF_CK(cudaMemcpyAsync(hoff.data(), out_offsets, hoff.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  SF_CK(cudaStreamSynchronize(st));
+  struct Item { int pab, pcd, flags; int64_t off; int str[4]; };
+  std::vector<std::vector<Item>> byc(kNumClass);
+  for (int64_t q = 0; q < nq; ++q) {
+    int s[4], pos[4] = {0, 1, 2, 3};
+    for (int k = 0; k < 4; ++k) {
+      s[k] = hq[4 * q + k];
+      if (s[k] < 0 || s[k] >= h->nshell) return fail(SF_EINVAL, "sf_eri_batch: shell index out of range");
+    }
+    int nc[4], so[4];
+    for (int k = 0; k < 4; ++k) nc[k] = ncart(h->l[s[k]]);
+    so[3] = 1;
+    so[2] = nc[3];
+    so[1] = nc[2] * nc[3];
+    so[0] = nc[1] * nc[2] * nc[3];
+    auto before = [&](int x, int y) { return h->l[x] < h->l[y] || (h->l[x] == h->l[y] && x < y); };
+    if (before(s[0], s[1])) { std::swap(s[0], s[1]); std::swap(pos[0], pos[1]); }
+    if (before(s[2], s[3])) { std::swap(s[2], s[3]); std::swap(pos[2], pos[3]); }
+    const int X = pair_class_of(h->l[s[0]], h->l[s[1]]), Y = pair_class_of(h->l[s[2]], h->l[s[3]]);
+    int x = X, y = Y;
+    if (X < Y) {
+      std::swap(s[0], s[2]); std::swap(s[1], s[3]);
+      std::swap(pos[0], pos[2]); std::swap(pos[1], pos[3]);
+      std::swap(x, y);
+    }
+    Item it;
+    it.pab = h->pairmap[(size_t)s[0] * h->nshell + s[1]];
+    it.pcd = h->pairmap[(size_t)s[2] * h->nshell + s[3]];
+    if (it.pab < 0 || it.pcd < 0) return fail(SF_EINVAL, "sf_eri_batch: internal pair lookup failed");
+    it.flags = 0;
+    it.off = hoff[q];
+    for (int k = 0; k < 4; ++k) it.str[k] = so[pos[k]];
+    byc[x * (x + 1) / 2 + y].push_back(it);
+  }
+  for (int cls = 0; cls < kNumClass; ++cls) {
+    const auto &v = byc[cls];
+    if (v.empty()) continue;
+    std::vector<int> pab(v.size()), pcd(v.size()), fl(v.size()), str(4 * v.size());
+    std::vector<int64_t> off(v.size());
+    for (size_t i = 0; i < v.size(); ++i) {
+      pab[i] = v[i].pab; pcd[i] = v[i].pcd; fl[i] = v[i].flags; off[i] = v[i].off;
+      for (int k = 0; k < 4; ++k) str[4 * i + k] = v[i].str[k];
+    }
+    DBuf<int> dpab, dpcd, dfl, dstr;
+    DBuf<int64_t> doff;
+    SF_CK(dpab.upload(pab)); SF_CK(dpcd.upload(pcd)); SF_CK(dfl.upload(fl)); SF_CK(dstr.upload(str));
+    SF_CK(doff.upload(off));
+    EriWork w{dpab.p, dpcd.p, dfl.p, doff.p, dstr.p, (int64_t)v.size(), out};
+    SF_CK(launch_eri(cls, precision == SF_PREC_FP32, h->kp, w, st));
+    SF_CK(cudaStreamSynchronize(st));
+  }
+  return SF_OK;
+}
+
+int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges, int32_t natom, double *S, double *T,
+                    double *V, void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_one_electron: NULL handle");
+  if (V && (natom < 0 || (natom > 0 && (!atom_xyz || !charges)))) return fail(SF_EINVAL, "sf_one_electron: bad atoms");
+  DeviceGuard g(h->device);
+  OneParams P;
+  P.sh = h->kp.sh;
+  P.exps = h->d_exps.p;
+  P.coefs = h->d_coefs.p;
+  P.poff = h->d_spoff.p;
+  P.nshell = h->nshell;
+  P.nao = h->nao;
+  P.atom_xyz = atom_xyz;
+  P.charges = charges;
+  P.natom = V ? natom : 0;
+  P.S = S;
+  P.T = T;
+  P.V = V;
+  SF_CK(launch_one_electron(P, (cudaStream_t)stream));
+  return SF_OK;
+}
+
+int sf_rys_roots_host(int32_t n, double x, int32_t fp32, double *u, double *w) {
+  if (n < 1 || n > kMaxRoots || !(x >= 0.0) || !u || !w) return fail(SF_EINVAL, "sf_rys_roots_host: bad arguments");
+  const HostTables &T = host_tables();
+  rys_eval_host(T.t64.data(), T.t32.data(), T.asym, n, x, fp32, u, w);
+  return SF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,36 @@
+// classes.h -- the 21 canonical shell-quartet classes (la lb | lc ld) with
+// l <= 2 and the thread-group size T used for each.  Class id = X(X+1)/2 + Y
+// for pair classes X >= Y (ss=0 ps=1 pp=2 ds=3 dp=4 dd=5).
+//   X(id, la, lb, lc, ld, T_fp64, T_fp32)
+#pragma once
+#define SF_CLASS_LIST(X)       \
+  X(0, 0, 0, 0, 0, 1, 1)       \
+  X(1, 1, 0, 0, 0, 1, 1)       \
+  X(2, 1, 0, 1, 0, 1, 1)       \
+  X(3, 1, 1, 0, 0, 1, 1)       \
+  X(4, 1, 1, 1, 0, 1, 1)       \
+  X(5, 1, 1, 1, 1, 4, 4)       \
+  X(6, 2, 0, 0, 0, 1, 1)       \
+  X(7, 2, 0, 1, 0, 1, 1)       \
+  X(8, 2, 0, 1, 1, 2, 2)       \
+  X(9, 2, 0, 2, 0, 2, 2)       \
+  X(10, 2, 1, 0, 0, 1, 1)      \
+  X(11, 2, 1, 1, 0, 2, 2)      \
+  X(12, 2, 1, 1, 1, 8, 8)      \
+  X(13, 2, 1, 2, 0, 4, 4)      \
+  X(14, 2, 1, 2, 1, 16, 16)    \
+  X(15, 2, 2, 0, 0, 2, 2)      \
+  X(16, 2, 2, 1, 0, 4, 4)      \
+  X(17, 2, 2, 1, 1, 16, 16)    \
+  X(18, 2, 2, 2, 0, 8, 8)      \
+  X(19, 2, 2, 2, 1, 32, 32)    \
+  X(20, 2, 2, 2, 2, 32, 32)
+
+namespace sf {
+struct ClassInfo { int la, lb, lc, ld, t64, t32; };
+constexpr ClassInfo kClassInfo[21] = {
+#define SF_CI(id, la, lb, lc, ld, t64, t32) {la, lb, lc, ld, t64, t32},
+    SF_CLASS_LIST(SF_CI)
+#undef SF_CI
+};
+}  // namespace sf

@@ -1,0 +1,43 @@
+// jk_f64.cu -- FP64 J/K kernels, one instantiation per class.
+#include "classes.h"
+#include "launch.h"
+
+namespace sf {
+
+template <int LA, int LB, int LC, int LD, int T>
+static cudaError_t run_jk64(const KParams &kp, const ClassWork &w, const double *D, double *Jh, double *Kh,
+                            cudaStream_t st) {
+  const int64_t n = w.q_end - w.q_begin;
+  if (n <= 0) return cudaSuccess;
+  constexpr int G = kBlock / T;
+  constexpr size_t smem = grp_smem<LA, LB, LC, LD, double, T>();
+  auto kern = jk_kernel<LA, LB, LC, LD, double, T>;
+  const int64_t grid = (n + G - 1) / G;
+  kern<<<(unsigned)grid, kBlock, smem, st>>>(kp, w, D, Jh, Kh);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jk_f64(int cls, const KParams &kp, const ClassWork &w, const double *D, double *Jh, double *Kh,
+                          cudaStream_t st) {
+  switch (cls) {
+#define SF_CASE(id, la, lb, lc, ld, t64, t32) \
+  case id: return run_jk64<la, lb, lc, ld, t64>(kp, w, D, Jh, Kh, st);
+    SF_CLASS_LIST(SF_CASE)
+#undef SF_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// raise the dynamic shared-memory limit of every group kernel on the current
+// device (called once per device by sf_create)
+cudaError_t prepare_jk_f64() {
+  cudaError_t e = cudaSuccess;
+#define SF_PREP(id, la, lb, lc, ld, t64, t32)                                                      \
+  if (e == cudaSuccess)                                                                            \
+    e = prep_smem(jk_kernel<la, lb, lc, ld, double, t64>, grp_smem<la, lb, lc, ld, double, t64>());
+  SF_CLASS_LIST(SF_PREP)
+#undef SF_PREP
+  return e;
+}
+
+}  // namespace sf

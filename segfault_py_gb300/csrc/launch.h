@@ -1,0 +1,44 @@
+// launch.h -- host-side launchers implemented in the kernel translation units.
+#pragma once
+#include "quartet.cuh"
+
+namespace sf {
+// J/K digestion kernels of class cls (0..20) over one work slice
+cudaError_t launch_jk_f64(int cls, const KParams &kp, const ClassWork &w, const double *D, double *Jh, double *Kh,
+                          cudaStream_t st);
+cudaError_t launch_jk_f32(int cls, const KParams &kp, const ClassWork &w, const float *D, double *Jh, double *Kh,
+                          cudaStream_t st);
+// raw integrals of one class
+cudaError_t launch_eri(int cls, int fp32, const KParams &kp, const EriWork &w, cudaStream_t st);
+// Schwarz bounds of pair class pc (0..5) over pairs [p0, p0+n)
+cudaError_t launch_schwarz(int pc, const KParams &kp, int p0, int n, double *qout, cudaStream_t st);
+
+cudaError_t prepare_jk_f64();
+cudaError_t prepare_jk_f32();
+cudaError_t prepare_eri();
+
+// one-electron kernel parameters (oneint.cu)
+struct OneParams {
+  DevShells sh;
+  const double *exps, *coefs;   // per shell primitives (shell prim offsets in poff)
+  const int *poff;
+  int nshell, nao;
+  const double *atom_xyz, *charges;
+  int natom;
+  double *S, *T, *V;
+};
+
+cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st);
+
+// smem bytes of a group kernel
+template <int LA, int LB, int LC, int LD, typename R, int T>
+constexpr size_t grp_smem() {
+  return T == 1 ? 0 : (size_t)(kBlock / T) * Grp<LA, LB, LC, LD, R, T>::BUFN * sizeof(R);
+}
+
+template <typename K>
+inline cudaError_t prep_smem(K kern, size_t smem) {
+  if (smem > 48 * 1024) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaSuccess;
+}
+}  // namespace sf

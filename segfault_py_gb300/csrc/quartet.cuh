@@ -1,0 +1,665 @@
+// quartet.cuh -- Rys-quadrature shell-quartet kernels (sm_103a).
+//
+// One canonical class (la lb | lc ld), la >= lb, lc >= ld, pair class of
+// (la,lb) >= pair class of (lc,ld), is one template instantiation.  A group of
+// T threads evaluates one contracted shell quartet:
+//
+//   (ab|cd)_{ia ib ic id} = sum_{prim quartets} sum_{r < n} Ix Iy Iz
+//
+// with n = floor(L/2)+1 roots (the reference always uses 5: core.f90:952).
+// For every primitive quartet and root the 2-D integrals of one Cartesian
+// direction come from the vertical recurrence of core.f90:815-874 (B00, B10,
+// B01, C00, C00') followed by the horizontal transfer of core.f90:877-899,
+// written as the equivalent two-term recursion I(a,b+1) = I(a+1,b) + AB I(a,b)
+// (bra) and the same on the ket.  The z direction carries the weight w_r and
+// the primitive prefactor, so the innermost statement of core.f90:961
+// (ix*iy*iz*w) costs one multiply and one FMA per Cartesian quadruple and root.
+//
+// T == 1: everything in registers, all indices compile-time.
+// T  > 1: the 3n 2-D tables of a primitive quartet are computed by the T
+//         threads in parallel (one (root, direction) task each), staged in
+//         shared memory, and every thread accumulates the Cartesian outputs
+//         o = t, t+T, t+2T, ...
+//
+// Epilogues: J/K digestion (fock), store (eri batch), diagonal max (Schwarz).
+#pragma once
+#include <cstdint>
+
+#include "sf_internal.h"
+
+namespace sf {
+
+struct KParams {
+  DevShells sh;
+  DevPairs pr;
+  DevPrims<double> p64;
+  DevPrims<float> p32;
+  const double *tab64;
+  const float *tab32;
+  RysAsym asym;
+  int nao;
+  int *err;            // device error flag (unused by the arithmetic kernels)
+};
+
+template <typename R>
+__device__ __forceinline__ const DevPrims<R> &prims_of(const KParams &kp);
+template <>
+__device__ __forceinline__ const DevPrims<double> &prims_of<double>(const KParams &kp) { return kp.p64; }
+template <>
+__device__ __forceinline__ const DevPrims<float> &prims_of<float>(const KParams &kp) { return kp.p32; }
+
+// 1/sqrt(a): single-precision hardware seed + two Newton-Raphson steps
+// y <- y (3/2 - a/2 y^2) (quadratic convergence: 2^-23 -> 2^-46 -> rounding).
+__device__ __forceinline__ double rsqrt_nr(double a) {
+  double y = (double)rsqrtf((float)a);
+  const double h = 0.5 * a;
+  y = y * (1.5 - h * y * y);
+  y = y * (1.5 - h * y * y);
+  return y;
+}
+__device__ __forceinline__ float rsqrt_nr(float a) { return rsqrtf(a); }
+
+template <typename R>
+struct TabDeg;
+template <>
+struct TabDeg<double> { static constexpr int v = kTabDeg64; };
+template <>
+struct TabDeg<float> { static constexpr int v = kTabDeg32; };
+
+template <typename R>
+__device__ __forceinline__ const R *tab_of(const KParams &kp);
+template <>
+__device__ __forceinline__ const double *tab_of<double>(const KParams &kp) { return kp.tab64; }
+template <>
+__device__ __forceinline__ const float *tab_of<float>(const KParams &kp) { return kp.tab32; }
+
+// all n roots (u = t^2) and weights at x
+template <int N, typename R>
+__device__ __forceinline__ void rys_roots_all(const KParams &kp, R x, R (&u)[N], R (&w)[N]) {
+  if (x >= (R)kTabXmax) {
+    const R ix = (R)1 / x, isx = rsqrt_nr(x);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      u[i] = (R)kp.asym.r[N][i] * ix;
+      w[i] = (R)kp.asym.w[N][i] * isx;
+    }
+    return;
+  }
+  constexpr int D = TabDeg<R>::v;
+  const int j = (int)x;
+  const R s = (R)2 * (x - (R)j) - (R)1;
+  const R *c = tab_of<R>(kp) + rys_tab_offset(N, D) + j * (D + 1) * 2 * N;
+#pragma unroll
+  for (int f = 0; f < N; ++f) {
+    u[f] = __ldg(c + D * 2 * N + f);
+    w[f] = __ldg(c + D * 2 * N + N + f);
+  }
+#pragma unroll
+  for (int k = D - 1; k >= 0; --k) {
+#pragma unroll
+    for (int f = 0; f < N; ++f) {
+      u[f] = u[f] * s + __ldg(c + k * 2 * N + f);
+      w[f] = w[f] * s + __ldg(c + k * 2 * N + N + f);
+    }
+  }
+}
+
+// one root r of the n-point rule
+template <int N, typename R>
+__device__ __forceinline__ void rys_root_one(const KParams &kp, R x, int r, R &u, R &w) {
+  if (x >= (R)kTabXmax) {
+    u = (R)kp.asym.r[N][r] / x;
+    w = (R)kp.asym.w[N][r] * rsqrt_nr(x);
+    return;
+  }
+  constexpr int D = TabDeg<R>::v;
+  const int j = (int)x;
+  const R s = (R)2 * (x - (R)j) - (R)1;
+  const R *c = tab_of<R>(kp) + rys_tab_offset(N, D) + j * (D + 1) * 2 * N;
+  u = __ldg(c + D * 2 * N + r);
+  w = __ldg(c + D * 2 * N + N + r);
+#pragma unroll
+  for (int k = D - 1; k >= 0; --k) {
+    u = u * s + __ldg(c + k * 2 * N + r);
+    w = w * s + __ldg(c + k * 2 * N + N + r);
+  }
+}
+
+template <int LA, int LB, int LC, int LD>
+struct QC {
+  static constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+  static constexpr int NCD = NC * ND, NABCD = NA * NB * NC * ND;
+  static constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
+  static constexpr int NR = L / 2 + 1;
+  static constexpr int SZ = (LA + 1) * (LB + 1) * (LC + 1) * (LD + 1);
+  __host__ __device__ static constexpr int ca(int o) { return o / (NB * NC * ND); }
+  __host__ __device__ static constexpr int cb(int o) { return (o / (NC * ND)) % NB; }
+  __host__ __device__ static constexpr int cc(int o) { return (o / ND) % NC; }
+  __host__ __device__ static constexpr int cd(int o) { return o % ND; }
+  // offset of output o's factor in the 2-D table of direction d
+  __host__ __device__ static constexpr int toff(int o, int d) {
+    return ((cart_e(LA, ca(o), d) * (LB + 1) + cart_e(LB, cb(o), d)) * (LC + 1) + cart_e(LC, cc(o), d)) * (LD + 1) +
+           cart_e(LD, cd(o), d);
+  }
+  __host__ __device__ static constexpr double norm(int o) {
+    return cart_norm(LA, ca(o)) * cart_norm(LB, cb(o)) * cart_norm(LC, cc(o)) * cart_norm(LD, cd(o));
+  }
+};
+
+// Vertical recurrence + horizontal transfer for one root and one direction.
+// Output I[((ia*(LB+1)+ib)*(LC+1)+ic)*(LD+1)+id].
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void rys_2d(R g0, R c00, R c00p, R b00, R b10, R b01, R ab, R cd,
+                                       R (&I)[QC<LA, LB, LC, LD>::SZ]) {
+  constexpr int LAB = LA + LB, LCD = LC + LD;
+  R G[LAB + 1][LCD + 1];
+  G[0][0] = g0;
+  if (LAB > 0) G[1][0] = c00 * g0;
+#pragma unroll
+  for (int i = 1; i < LAB; ++i) G[i + 1][0] = (R)i * b10 * G[i - 1][0] + c00 * G[i][0];
+  if (LCD > 0) {
+    G[0][1] = c00p * g0;
+#pragma unroll
+    for (int i = 1; i <= LAB; ++i) G[i][1] = (R)i * b00 * G[i - 1][0] + c00p * G[i][0];
+#pragma unroll
+    for (int k = 1; k < LCD; ++k) {
+      G[0][k + 1] = (R)k * b01 * G[0][k - 1] + c00p * G[0][k];
+#pragma unroll
+      for (int i = 1; i <= LAB; ++i)
+        G[i][k + 1] = (R)k * b01 * G[i][k - 1] + (R)i * b00 * G[i - 1][k] + c00p * G[i][k];
+    }
+  }
+  // bra transfer: H[ia][ib][k]
+  R H[LA + 1][LB + 1][LCD + 1];
+#pragma unroll
+  for (int k = 0; k <= LCD; ++k) {
+    R t[LAB + 1];
+#pragma unroll
+    for (int i = 0; i <= LAB; ++i) t[i] = G[i][k];
+#pragma unroll
+    for (int ia = 0; ia <= LA; ++ia) H[ia][0][k] = t[ia];
+#pragma unroll
+    for (int ib = 1; ib <= LB; ++ib) {
+#pragma unroll
+      for (int i = 0; i <= LAB - ib; ++i) t[i] = t[i + 1] + ab * t[i];
+#pragma unroll
+      for (int ia = 0; ia <= LA; ++ia) H[ia][ib][k] = t[ia];
+    }
+  }
+  // ket transfer
+#pragma unroll
+  for (int ia = 0; ia <= LA; ++ia) {
+#pragma unroll
+    for (int ib = 0; ib <= LB; ++ib) {
+      R t[LCD + 1];
+#pragma unroll
+      for (int k = 0; k <= LCD; ++k) t[k] = H[ia][ib][k];
+#pragma unroll
+      for (int ic = 0; ic <= LC; ++ic) I[((ia * (LB + 1) + ib) * (LC + 1) + ic) * (LD + 1) + 0] = t[ic];
+#pragma unroll
+      for (int id = 1; id <= LD; ++id) {
+#pragma unroll
+        for (int k = 0; k <= LCD - id; ++k) t[k] = t[k + 1] + cd * t[k];
+#pragma unroll
+        for (int ic = 0; ic <= LC; ++ic) I[((ia * (LB + 1) + ib) * (LC + 1) + ic) * (LD + 1) + id] = t[ic];
+      }
+    }
+  }
+}
+
+// geometry of one contracted quartet
+template <typename R>
+struct QGeom {
+  int a, b, c, d;
+  int ab_off, ab_n, cd_off, cd_n;
+  R Ax, Ay, Az, Cx, Cy, Cz;
+  R ABx, ABy, ABz, CDx, CDy, CDz;
+};
+
+template <typename R>
+__device__ __forceinline__ QGeom<R> make_geom(const KParams &kp, int pab, int pcd, bool swap_ab, bool swap_cd) {
+  QGeom<R> g;
+  int a = kp.pr.a[pab], b = kp.pr.b[pab], c = kp.pr.a[pcd], d = kp.pr.b[pcd];
+  if (swap_ab) { int t = a; a = b; b = t; }
+  if (swap_cd) { int t = c; c = d; d = t; }
+  g.a = a; g.b = b; g.c = c; g.d = d;
+  g.ab_off = kp.pr.poff[pab]; g.ab_n = kp.pr.np[pab];
+  g.cd_off = kp.pr.poff[pcd]; g.cd_n = kp.pr.np[pcd];
+  const double ax = kp.sh.cx[a], ay = kp.sh.cy[a], az = kp.sh.cz[a];
+  const double bx = kp.sh.cx[b], by = kp.sh.cy[b], bz = kp.sh.cz[b];
+  const double cx = kp.sh.cx[c], cy = kp.sh.cy[c], cz = kp.sh.cz[c];
+  const double dx = kp.sh.cx[d], dy = kp.sh.cy[d], dz = kp.sh.cz[d];
+  g.Ax = (R)ax; g.Ay = (R)ay; g.Az = (R)az;
+  g.Cx = (R)cx; g.Cy = (R)cy; g.Cz = (R)cz;
+  g.ABx = (R)(ax - bx); g.ABy = (R)(ay - by); g.ABz = (R)(az - bz);
+  g.CDx = (R)(cx - dx); g.CDy = (R)(cy - dy); g.CDz = (R)(cz - dz);
+  return g;
+}
+
+// scalars of one primitive quartet
+template <typename R>
+struct PQ {
+  R pax, pay, paz, qcx, qcy, qcz, pqx, pqy, pqz;
+  R r2, aq, ap, i2p, i2q, x, pref;
+};
+
+template <typename R>
+__device__ __forceinline__ void load_prim_ab(const KParams &kp, const QGeom<R> &g, int ip, PQ<R> &s, R &p, R &px,
+                                             R &py, R &pz, R &kab) {
+  const DevPrims<R> &P = prims_of<R>(kp);
+  const int i = g.ab_off + ip;
+  p = __ldg(P.p + i); px = __ldg(P.px + i); py = __ldg(P.py + i); pz = __ldg(P.pz + i);
+  kab = __ldg(P.k + i); s.i2p = __ldg(P.inv2p + i);
+  s.pax = px - g.Ax; s.pay = py - g.Ay; s.paz = pz - g.Az;
+}
+
+template <typename R>
+__device__ __forceinline__ void load_prim_cd(const KParams &kp, const QGeom<R> &g, int iq, PQ<R> &s, R p, R px, R py,
+                                             R pz, R kab) {
+  const DevPrims<R> &P = prims_of<R>(kp);
+  const int i = g.cd_off + iq;
+  const R q = __ldg(P.p + i), qx = __ldg(P.px + i), qy = __ldg(P.py + i), qz = __ldg(P.pz + i);
+  const R kcd = __ldg(P.k + i);
+  s.i2q = __ldg(P.inv2p + i);
+  s.qcx = qx - g.Cx; s.qcy = qy - g.Cy; s.qcz = qz - g.Cz;
+  s.pqx = px - qx; s.pqy = py - qy; s.pqz = pz - qz;
+  const R rr = rsqrt_nr(p + q);
+  s.r2 = rr * rr;
+  s.aq = q * s.r2;
+  s.ap = p * s.r2;
+  const R rho = p * s.aq;
+  s.x = rho * (s.pqx * s.pqx + s.pqy * s.pqy + s.pqz * s.pqz);
+  s.pref = kab * kcd * rr;
+}
+
+// ---------------------------------------------------------------------------
+// T == 1: whole quartet in registers; acc[o] unnormalised
+// ---------------------------------------------------------------------------
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R (&acc)[QC<LA, LB, LC, LD>::NABCD]) {
+  using Q = QC<LA, LB, LC, LD>;
+  constexpr int NR = Q::NR, SZ = Q::SZ;
+#pragma unroll
+  for (int o = 0; o < Q::NABCD; ++o) acc[o] = (R)0;
+  for (int ip = 0; ip < g.ab_n; ++ip) {
+    PQ<R> s;
+    R p, px, py, pz, kab;
+    load_prim_ab<R>(kp, g, ip, s, p, px, py, pz, kab);
+    for (int iq = 0; iq < g.cd_n; ++iq) {
+      load_prim_cd<R>(kp, g, iq, s, p, px, py, pz, kab);
+      R u[NR], w[NR];
+      rys_roots_all<NR, R>(kp, s.x, u, w);
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const R uu = u[r];
+        const R b00 = (R)0.5 * s.r2 * uu;
+        const R b10 = s.i2p * ((R)1 - s.aq * uu);
+        const R b01 = s.i2q * ((R)1 - s.ap * uu);
+        const R tq = s.aq * uu, tp = s.ap * uu;
+        R Ix[SZ], Iy[SZ], Iz[SZ];
+        rys_2d<LA, LB, LC, LD, R>((R)1, s.pax - tq * s.pqx, s.qcx + tp * s.pqx, b00, b10, b01, g.ABx, g.CDx, Ix);
+        rys_2d<LA, LB, LC, LD, R>((R)1, s.pay - tq * s.pqy, s.qcy + tp * s.pqy, b00, b10, b01, g.ABy, g.CDy, Iy);
+        rys_2d<LA, LB, LC, LD, R>(s.pref * w[r], s.paz - tq * s.pqz, s.qcz + tp * s.pqz, b00, b10, b01, g.ABz,
+                                  g.CDz, Iz);
+#pragma unroll
+        for (int o = 0; o < Q::NABCD; ++o) acc[o] += Ix[Q::toff(o, 0)] * Iy[Q::toff(o, 1)] * Iz[Q::toff(o, 2)];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// T > 1: group of T lanes (inside one warp); tab = 3*NR*SZ shared values
+// ---------------------------------------------------------------------------
+template <int LA, int LB, int LC, int LD, typename R, int T>
+struct Grp {
+  using Q = QC<LA, LB, LC, LD>;
+  static constexpr int NPER = (Q::NABCD + T - 1) / T;
+  static constexpr int TABN = 3 * Q::NR * Q::SZ;
+  static constexpr int BUFN = TABN > Q::NABCD ? TABN : Q::NABCD;
+};
+
+template <int LA, int LB, int LC, int LD, typename R, int T>
+__device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R *tab, int t, unsigned gmask,
+                                         R (&acc)[Grp<LA, LB, LC, LD, R, T>::NPER]) {
+  using Q = QC<LA, LB, LC, LD>;
+  using GP = Grp<LA, LB, LC, LD, R, T>;
+  constexpr int NR = Q::NR, SZ = Q::SZ, NPER = GP::NPER;
+  int off[NPER];
+#pragma unroll
+  for (int k = 0; k < NPER; ++k) {
+    const int o = t + k * T;
+    acc[k] = (R)0;
+    off[k] = o < Q::NABCD ? (Q::toff(o, 0) | ((NR * SZ + Q::toff(o, 1)) << 10) |
+                             ((2 * NR * SZ + Q::toff(o, 2)) << 20))
+                          : 0;
+  }
+  for (int ip = 0; ip < g.ab_n; ++ip) {
+    PQ<R> s;
+    R p, px, py, pz, kab;
+    load_prim_ab<R>(kp, g, ip, s, p, px, py, pz, kab);
+    for (int iq = 0; iq < g.cd_n; ++iq) {
+      load_prim_cd<R>(kp, g, iq, s, p, px, py, pz, kab);
+      for (int task = t; task < 3 * NR; task += T) {
+        const int r = task % NR, d = task / NR;
+        R uu, ww;
+        rys_root_one<NR, R>(kp, s.x, r, uu, ww);
+        const R b00 = (R)0.5 * s.r2 * uu;
+        const R b10 = s.i2p * ((R)1 - s.aq * uu);
+        const R b01 = s.i2q * ((R)1 - s.ap * uu);
+        const R tq = s.aq * uu, tp = s.ap * uu;
+        const R pa = d == 0 ? s.pax : d == 1 ? s.pay : s.paz;
+        const R qc = d == 0 ? s.qcx : d == 1 ? s.qcy : s.qcz;
+        const R pq = d == 0 ? s.pqx : d == 1 ? s.pqy : s.pqz;
+        const R ab = d == 0 ? g.ABx : d == 1 ? g.ABy : g.ABz;
+        const R cd = d == 0 ? g.CDx : d == 1 ? g.CDy : g.CDz;
+        const R g0 = d == 2 ? s.pref * ww : (R)1;
+        R I[SZ];
+        rys_2d<LA, LB, LC, LD, R>(g0, pa - tq * pq, qc + tp * pq, b00, b10, b01, ab, cd, I);
+        R *dst = tab + (d * NR + r) * SZ;
+#pragma unroll
+        for (int i = 0; i < SZ; ++i) dst[i] = I[i];
+      }
+      __syncwarp(gmask);
+#pragma unroll
+      for (int k = 0; k < NPER; ++k) {
+        if (t + k * T < Q::NABCD) {
+          const int ox = off[k] & 1023, oy = (off[k] >> 10) & 1023, oz = off[k] >> 20;
+          R v = (R)0;
+#pragma unroll
+          for (int r = 0; r < NR; ++r) v += tab[ox + r * SZ] * tab[oy + r * SZ] * tab[oz + r * SZ];
+          acc[k] += v;
+        }
+      }
+      __syncwarp(gmask);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// J/K digestion.  With v = degeneracy-scaled normalised integral of the
+// component quadruple (i,j,k,l) of a canonical shell quartet, the eight index
+// permutations of hf.py:49-60 give J = Jh + Jh^T and K = Kh + Kh^T with
+//   Jh_ij += 2 v D_kl, Jh_kl += 2 v D_ij,
+//   Kh_ik += v D_jl, Kh_jk += v D_il, Kh_il += v D_jk, Kh_jl += v D_ik.
+// ---------------------------------------------------------------------------
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, const R (&acc)[QC<LA, LB, LC, LD>::NABCD],
+                                          double scale, const R *__restrict__ D, double *Jh, double *Kh) {
+  using Q = QC<LA, LB, LC, LD>;
+  const int n = kp.nao;
+  const int a0 = kp.sh.ao[g.a], b0 = kp.sh.ao[g.b], c0 = kp.sh.ao[g.c], d0 = kp.sh.ao[g.d];
+  R v[Q::NABCD];
+#pragma unroll
+  for (int o = 0; o < Q::NABCD; ++o) v[o] = acc[o] * (R)Q::norm(o);
+  // J_ab and K blocks need D of the other pairs
+#pragma unroll
+  for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+    for (int ib = 0; ib < Q::NB; ++ib) {
+      R s = 0;
+#pragma unroll
+      for (int ic = 0; ic < Q::NC; ++ic)
+#pragma unroll
+        for (int id = 0; id < Q::ND; ++id)
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (c0 + ic) * n + d0 + id);
+      atomicAdd(Jh + (a0 + ia) * n + b0 + ib, 2.0 * scale * (double)s);
+    }
+#pragma unroll
+  for (int ic = 0; ic < Q::NC; ++ic)
+#pragma unroll
+    for (int id = 0; id < Q::ND; ++id) {
+      R s = 0;
+#pragma unroll
+      for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+        for (int ib = 0; ib < Q::NB; ++ib)
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + b0 + ib);
+      atomicAdd(Jh + (c0 + ic) * n + d0 + id, 2.0 * scale * (double)s);
+    }
+#pragma unroll
+  for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+    for (int ic = 0; ic < Q::NC; ++ic) {
+      R s = 0;
+#pragma unroll
+      for (int ib = 0; ib < Q::NB; ++ib)
+#pragma unroll
+        for (int id = 0; id < Q::ND; ++id)
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (b0 + ib) * n + d0 + id);
+      atomicAdd(Kh + (a0 + ia) * n + c0 + ic, scale * (double)s);
+    }
+#pragma unroll
+  for (int ib = 0; ib < Q::NB; ++ib)
+#pragma unroll
+    for (int ic = 0; ic < Q::NC; ++ic) {
+      R s = 0;
+#pragma unroll
+      for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+        for (int id = 0; id < Q::ND; ++id)
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + d0 + id);
+      atomicAdd(Kh + (b0 + ib) * n + c0 + ic, scale * (double)s);
+    }
+#pragma unroll
+  for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+    for (int id = 0; id < Q::ND; ++id) {
+      R s = 0;
+#pragma unroll
+      for (int ib = 0; ib < Q::NB; ++ib)
+#pragma unroll
+        for (int ic = 0; ic < Q::NC; ++ic)
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (b0 + ib) * n + c0 + ic);
+      atomicAdd(Kh + (a0 + ia) * n + d0 + id, scale * (double)s);
+    }
+#pragma unroll
+  for (int ib = 0; ib < Q::NB; ++ib)
+#pragma unroll
+    for (int id = 0; id < Q::ND; ++id) {
+      R s = 0;
+#pragma unroll
+      for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+        for (int ic = 0; ic < Q::NC; ++ic)
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + c0 + ic);
+      atomicAdd(Kh + (b0 + ib) * n + d0 + id, scale * (double)s);
+    }
+}
+
+// group version: normalised integrals are staged in buf (shared), then the
+// 6 blocks' entries are distributed over the T lanes
+template <int LA, int LB, int LC, int LD, typename R, int T>
+__device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
+                                           const R (&acc)[Grp<LA, LB, LC, LD, R, T>::NPER], R *buf, int t,
+                                           unsigned gmask, double scale, const R *__restrict__ D, double *Jh,
+                                           double *Kh) {
+  using Q = QC<LA, LB, LC, LD>;
+  constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
+  const int n = kp.nao;
+  const int a0 = kp.sh.ao[g.a], b0 = kp.sh.ao[g.b], c0 = kp.sh.ao[g.c], d0 = kp.sh.ao[g.d];
+  __syncwarp(gmask);
+#pragma unroll
+  for (int k = 0; k < Grp<LA, LB, LC, LD, R, T>::NPER; ++k) {
+    const int o = t + k * T;
+    if (o < Q::NABCD) buf[o] = acc[k] * (R)Q::norm(o);
+  }
+  __syncwarp(gmask);
+  constexpr int E0 = NA * NB, E1 = E0 + NC * ND, E2 = E1 + NA * NC, E3 = E2 + NB * NC, E4 = E3 + NA * ND,
+                E5 = E4 + NB * ND;
+#define V4(ia, ib, ic, id) buf[(((ia) * NB + (ib)) * NC + (ic)) * ND + (id)]
+  for (int e = t; e < E5; e += T) {
+    R s = 0;
+    if (e < E0) {
+      const int ia = e / NB, ib = e % NB;
+      for (int ic = 0; ic < NC; ++ic)
+        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (c0 + ic) * n + d0 + id);
+      atomicAdd(Jh + (a0 + ia) * n + b0 + ib, 2.0 * scale * (double)s);
+    } else if (e < E1) {
+      const int ic = (e - E0) / ND, id = (e - E0) % ND;
+      for (int ia = 0; ia < NA; ++ia)
+        for (int ib = 0; ib < NB; ++ib) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + b0 + ib);
+      atomicAdd(Jh + (c0 + ic) * n + d0 + id, 2.0 * scale * (double)s);
+    } else if (e < E2) {
+      const int ia = (e - E1) / NC, ic = (e - E1) % NC;
+      for (int ib = 0; ib < NB; ++ib)
+        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (b0 + ib) * n + d0 + id);
+      atomicAdd(Kh + (a0 + ia) * n + c0 + ic, scale * (double)s);
+    } else if (e < E3) {
+      const int ib = (e - E2) / NC, ic = (e - E2) % NC;
+      for (int ia = 0; ia < NA; ++ia)
+        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + d0 + id);
+      atomicAdd(Kh + (b0 + ib) * n + c0 + ic, scale * (double)s);
+    } else if (e < E4) {
+      const int ia = (e - E3) / ND, id = (e - E3) % ND;
+      for (int ib = 0; ib < NB; ++ib)
+        for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * __ldg(D + (b0 + ib) * n + c0 + ic);
+      atomicAdd(Kh + (a0 + ia) * n + d0 + id, scale * (double)s);
+    } else {
+      const int ib = (e - E4) / ND, id = (e - E4) % ND;
+      for (int ia = 0; ia < NA; ++ia)
+        for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + c0 + ic);
+      atomicAdd(Kh + (b0 + ib) * n + d0 + id, scale * (double)s);
+    }
+  }
+#undef V4
+}
+
+// ---------------------------------------------------------------------------
+// work description of one (class, precision) slice of the implicit quartet
+// list: for bra pair i (class X, sorted by Q), the ket pairs are j in
+// [jstart[i], jstart[i] + prefix[i+1] - prefix[i]) of class Y.
+// ---------------------------------------------------------------------------
+struct ClassWork {
+  const int64_t *prefix;   // nX + 1
+  const int *jstart;       // nX, or null (= 0)
+  int64_t q_begin, q_end;  // slice of [0, prefix[nX])
+  int nX;
+  int x0, y0;              // first global pair index of class X / Y
+  int same;                // X == Y
+};
+
+__device__ __forceinline__ void decode_quartet(const ClassWork &w, int64_t q, int &i, int &j) {
+  int lo = 0, hi = w.nX;   // prefix[lo] <= q < prefix[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(w.prefix + mid) <= q) lo = mid; else hi = mid;
+  }
+  i = lo;
+  j = (w.jstart ? __ldg(w.jstart + lo) : 0) + (int)(q - __ldg(w.prefix + lo));
+}
+
+constexpr int kBlock = 128;
+
+template <int LA, int LB, int LC, int LD, typename R, int T>
+__global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, const R *__restrict__ D, double *Jh,
+                                                    double *Kh) {
+  constexpr int G = kBlock / T;
+  const int grp = threadIdx.x / T, t = threadIdx.x % T;
+  const int64_t q = w.q_begin + (int64_t)blockIdx.x * G + grp;
+  if (q >= w.q_end) return;
+  int i, j;
+  decode_quartet(w, q, i, j);
+  const int pab = w.x0 + i, pcd = w.y0 + j;
+  const QGeom<R> g = make_geom<R>(kp, pab, pcd, false, false);
+  double scale = 1.0;
+  if (g.a == g.b) scale *= 0.5;
+  if (g.c == g.d) scale *= 0.5;
+  if (w.same && i == j) scale *= 0.5;
+  if constexpr (T == 1) {
+    R acc[QC<LA, LB, LC, LD>::NABCD];
+    eval_t1<LA, LB, LC, LD, R>(kp, g, acc);
+    digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh);
+  } else {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using GP = Grp<LA, LB, LC, LD, R, T>;
+    R *buf = reinterpret_cast<R *>(smem_raw) + grp * GP::BUFN;
+    const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1)));
+    R acc[GP::NPER];
+    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc);
+    digest_grp<LA, LB, LC, LD, R, T>(kp, g, acc, buf, t, gmask, scale, D, Jh, Kh);
+  }
+}
+
+// raw integrals of an explicit quartet list (one class); perm packs, per
+// canonical slot s (a,b,c,d), the original position (2 bits each) plus the
+// swap flags of the bra / ket shells (bits 8, 9)
+struct EriWork {
+  const int *pab, *pcd;        // canonical pair indices
+  const int *flags;            // bit0 swap a<->b, bit1 swap c<->d (within the pair record)
+  const int64_t *out_off;      // output offset per quartet
+  const int *strides;          // 4 output strides per quartet (canonical slot order)
+  int64_t n;
+  double *out;
+};
+
+template <int LA, int LB, int LC, int LD, typename R, int T>
+__global__ void __launch_bounds__(kBlock) eri_kernel(KParams kp, EriWork w) {
+  using Q = QC<LA, LB, LC, LD>;
+  constexpr int G = kBlock / T;
+  const int grp = threadIdx.x / T, t = threadIdx.x % T;
+  const int64_t q = (int64_t)blockIdx.x * G + grp;
+  if (q >= w.n) return;
+  const int fl = w.flags[q];
+  const QGeom<R> g = make_geom<R>(kp, w.pab[q], w.pcd[q], fl & 1, fl & 2);
+  const int s0 = w.strides[4 * q], s1 = w.strides[4 * q + 1], s2 = w.strides[4 * q + 2], s3 = w.strides[4 * q + 3];
+  double *out = w.out + w.out_off[q];
+  if constexpr (T == 1) {
+    R acc[Q::NABCD];
+    eval_t1<LA, LB, LC, LD, R>(kp, g, acc);
+#pragma unroll
+    for (int o = 0; o < Q::NABCD; ++o)
+      out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = (double)(acc[o] * (R)Q::norm(o));
+  } else {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using GP = Grp<LA, LB, LC, LD, R, T>;
+    R *buf = reinterpret_cast<R *>(smem_raw) + grp * GP::BUFN;
+    const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1)));
+    R acc[GP::NPER];
+    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc);
+#pragma unroll
+    for (int k = 0; k < GP::NPER; ++k) {
+      const int o = t + k * T;
+      if (o < Q::NABCD)
+        out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = (double)(acc[k] * (R)Q::norm(o));
+    }
+  }
+}
+
+// Schwarz: Q_ab = sqrt(max_{ia,ib} |(ia ib|ia ib)|) over the pairs
+// [p0, p0 + n) of one pair class; class (X|X)
+template <int LA, int LB, typename R, int T>
+__global__ void __launch_bounds__(kBlock) schwarz_kernel(KParams kp, int p0, int n, double *qout) {
+  using Q = QC<LA, LB, LA, LB>;
+  constexpr int G = kBlock / T;
+  const int grp = threadIdx.x / T, t = threadIdx.x % T;
+  const int i = blockIdx.x * G + grp;
+  if (i >= n) return;
+  const QGeom<R> g = make_geom<R>(kp, p0 + i, p0 + i, false, false);
+  double m = 0.0;
+  if constexpr (T == 1) {
+    R acc[Q::NABCD];
+    eval_t1<LA, LB, LA, LB, R>(kp, g, acc);
+#pragma unroll
+    for (int o = 0; o < Q::NABCD; ++o)
+      if (Q::ca(o) == Q::cc(o) && Q::cb(o) == Q::cd(o)) m = fmax(m, fabs((double)(acc[o] * (R)Q::norm(o))));
+  } else {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using GP = Grp<LA, LB, LA, LB, R, T>;
+    R *buf = reinterpret_cast<R *>(smem_raw) + grp * GP::BUFN;
+    const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1)));
+    R acc[GP::NPER];
+    eval_grp<LA, LB, LA, LB, R, T>(kp, g, buf, t, gmask, acc);
+#pragma unroll
+    for (int k = 0; k < GP::NPER; ++k) {
+      const int o = t + k * T;
+      if (o < Q::NABCD && Q::ca(o) == Q::cc(o) && Q::cb(o) == Q::cd(o))
+        m = fmax(m, fabs((double)(acc[k] * (R)Q::norm(o))));
+    }
+#pragma unroll
+    for (int sft = T / 2; sft > 0; sft >>= 1) m = fmax(m, __shfl_xor_sync(gmask, m, sft, T));
+  }
+  if (t == 0) qout[p0 + i] = sqrt(m);
+}
+
+}  // namespace sf

@@ -1,0 +1,262 @@
+"""The GPU Fock build behind the reference's ERI/Fock boundary.
+
+Reference boundary (src/hf/hf.py):
+* ``rys.eri_rys(...)`` per unique AO quartet (hf.py:26-30, core.f90:967-1002)
+* ``build_eri_parallel(cgfs, ncgf)`` -> dense (N,N,N,N) tensor (hf.py:33-61)
+* ``G = einsum('pqrs,rs') - 0.5 einsum('prqs,rs')`` each SCF iteration (hf.py:300)
+
+Here:
+* ``FockBuilder(mol).jk(D) -> (J, K)``: direct, Schwarz-screened J/K on the
+  GPU (G = J - K/2), no N^4 tensor.  FP64, FP32 or mixed precision.
+* ``FockBuilder(mol).build_eri()``: the dense tensor of build_eri_parallel,
+  from the same GPU integrals (small molecules only: N^4 doubles).
+* ``eri_rys(c1..c4, e1..e4, s1..s4, n1..n4, r1..r4)``: the 20-argument call of
+  rys.eri_rys, evaluated by the GPU kernels.
+* ``FockBuilder(mol).one_electron() -> (S, T, V)`` (hf.py:266-274).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .molecule import Molecule
+
+DEFAULT_CUTOFF = 1e-12        # Schwarz cutoff on Q_ab Q_cd
+DEFAULT_FP32_CUTOFF = 1e-5    # mixed precision: Q_ab Q_cd below this run in FP32
+
+
+def _stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _ptr(t: torch.Tensor):
+    return C.c_void_p(t.data_ptr())
+
+
+def shell_descs(table: dict):
+    """Shell table (Molecule.shell_table) -> ctypes array; returns (array, keepalive)."""
+    n = len(table["l"])
+    arr = (_lib.ShellDesc * n)()
+    exps = np.ascontiguousarray(table["exps"], dtype=np.float64)
+    coefs = np.ascontiguousarray(table["coefs"], dtype=np.float64)
+    for s in range(n):
+        o = int(table["prim_offset"][s])
+        d = arr[s]
+        d.l = int(table["l"][s])
+        d.nprim = int(table["nprim"][s])
+        d.atom = int(table["atom"][s])
+        d.ao_offset = int(table["ao_offset"][s])
+        for k in range(3):
+            d.center[k] = float(table["center"][s][k])
+        d.exps = exps[o:].ctypes.data_as(C.POINTER(C.c_double))
+        d.coefs = coefs[o:].ctypes.data_as(C.POINTER(C.c_double))
+    return arr, (exps, coefs)
+
+
+class FockBuilder:
+    """Direct-SCF J/K builder for one molecule on the current CUDA device."""
+
+    def __init__(self, mol: Molecule | dict, device: str | torch.device = "cuda", cutoff: float = DEFAULT_CUTOFF,
+                 fp32_cutoff: float = DEFAULT_FP32_CUTOFF, precision: str = "fp64"):
+        L = _lib.lib()
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("FockBuilder needs a CUDA device")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        self.mol = mol if isinstance(mol, Molecule) else None
+        table = mol.shell_table() if isinstance(mol, Molecule) else mol
+        self.table = table
+        self.cutoff = cutoff
+        self.fp32_cutoff = fp32_cutoff
+        self.precision = precision
+        arr, keep = shell_descs(table)
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            torch.cuda.current_stream().synchronize()
+            _lib.check(L.sf_create(C.cast(arr, C.c_void_p), len(arr), C.byref(h)))
+        self._h = h
+        del keep
+        self.nao = L.sf_nao(h)
+        self.nshell = len(table["l"])
+        self.l = np.asarray(table["l"])
+        self.ao_offset = np.asarray(table["ao_offset"])
+        self.q = self.schwarz()
+        self.last_stats = None
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().sf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def schwarz(self) -> np.ndarray:
+        q = np.zeros((self.nshell, self.nshell))
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().sf_schwarz(self._h, q.ctypes.data, _stream_ptr()))
+        return q
+
+    def set_partition(self, part: int, nparts: int):
+        _lib.check(_lib.lib().sf_set_partition(self._h, part, nparts))
+
+    # ------------------------------------------------------------------
+    def jk(self, D: torch.Tensor, precision: str | None = None, cutoff: float | None = None,
+           fp32_cutoff: float | None = None, out=None, stats: bool = False):
+        """J_pq = sum (pq|rs) D_rs and K_pq = sum (pr|qs) D_rs for symmetric D."""
+        prec = _lib.PRECISION[precision or self.precision]
+        n = self.nao
+        if D.shape != (n, n) or D.dtype != torch.float64 or D.device != self.device:
+            raise ValueError("D must be a (%d,%d) float64 tensor on %s" % (n, n, self.device))
+        D = D.contiguous()
+        if out is None:
+            J = torch.empty((n, n), dtype=torch.float64, device=self.device)
+            K = torch.empty((n, n), dtype=torch.float64, device=self.device)
+        else:
+            J, K = out
+        st = _lib.Stats() if stats else None
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().sf_fock_jk(self._h, _ptr(D), _ptr(J), _ptr(K), prec,
+                                             self.cutoff if cutoff is None else cutoff,
+                                             self.fp32_cutoff if fp32_cutoff is None else fp32_cutoff,
+                                             C.byref(st) if st is not None else None, _stream_ptr()))
+        if st is not None:
+            self.last_stats = st.as_dict()
+        return J, K
+
+    def set_profiling(self, on: bool = True):
+        _lib.check(_lib.lib().sf_set_profiling(self._h, 1 if on else 0))
+
+    def slice_info(self):
+        """Per-launch work and (when profiling) device time of the last Fock build."""
+        L = _lib.lib()
+        out = []
+        for i in range(L.sf_slice_count(self._h)):
+            si = _lib.SliceInfo()
+            _lib.check(L.sf_get_slice_info(self._h, i, C.byref(si)))
+            out.append(si.as_dict())
+        return out
+
+    def fock(self, H: torch.Tensor, D: torch.Tensor, **kw):
+        """F = H + J - K/2 (hf.py:300-301)."""
+        J, K = self.jk(D, **kw)
+        return H + J - 0.5 * K
+
+    # ------------------------------------------------------------------
+    def eri_quartets(self, quartets, precision: str = "fp64"):
+        """Contracted integrals of shell quartets (nq,4): list of (na,nb,nc,nd) arrays."""
+        q = np.ascontiguousarray(quartets, dtype=np.int32).reshape(-1, 4)
+        nc = (self.l + 1) * (self.l + 2) // 2
+        sizes = np.prod(nc[q], axis=1).astype(np.int64)
+        offs = np.zeros(len(q), dtype=np.int64)
+        if len(q):
+            offs[1:] = np.cumsum(sizes)[:-1]
+        total = int(sizes.sum())
+        dq = torch.from_numpy(q).to(self.device)
+        do = torch.from_numpy(offs).to(self.device)
+        out = torch.zeros(max(total, 1), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().sf_eri_batch(self._h, _ptr(dq), len(q), _lib.PRECISION[precision], _ptr(out),
+                                               _ptr(do), _stream_ptr()))
+        flat = out.cpu().numpy()
+        return [flat[o:o + s].reshape(tuple(nc[row])) for o, s, row in zip(offs, sizes, q)]
+
+    def build_eri(self, precision: str = "fp64") -> np.ndarray:
+        """Dense (N,N,N,N) tensor as build_eri_parallel (hf.py:33-61); small N only."""
+        n = self.nao
+        ns = self.nshell
+        quartets = []
+        for a in range(ns):
+            for b in range(a + 1):
+                for c in range(ns):
+                    for d in range(c + 1):
+                        if a * (a + 1) // 2 + b >= c * (c + 1) // 2 + d:
+                            quartets.append((a, b, c, d))
+        blocks = self.eri_quartets(np.array(quartets, dtype=np.int32), precision)
+        E = np.zeros((n, n, n, n))
+        o = self.ao_offset
+        for (a, b, c, d), blk in zip(quartets, blocks):
+            sa, sb, sc, sd = (slice(o[x], o[x] + blk.shape[k]) for k, x in enumerate((a, b, c, d)))
+            E[sa, sb, sc, sd] = blk
+            E[sb, sa, sc, sd] = blk.transpose(1, 0, 2, 3)
+            E[sa, sb, sd, sc] = blk.transpose(0, 1, 3, 2)
+            E[sb, sa, sd, sc] = blk.transpose(1, 0, 3, 2)
+            E[sc, sd, sa, sb] = blk.transpose(2, 3, 0, 1)
+            E[sd, sc, sa, sb] = blk.transpose(3, 2, 0, 1)
+            E[sc, sd, sb, sa] = blk.transpose(2, 3, 1, 0)
+            E[sd, sc, sb, sa] = blk.transpose(3, 2, 1, 0)
+        return E
+
+    # ------------------------------------------------------------------
+    def one_electron(self, atom_xyz=None, charges=None):
+        """S, T, V (hf.py:266-274); nuclei default to the molecule's atoms."""
+        if atom_xyz is None:
+            atom_xyz, charges = self.mol.atom_table()
+        n = self.nao
+        xyz = torch.as_tensor(np.ascontiguousarray(atom_xyz, dtype=np.float64), device=self.device)
+        Z = torch.as_tensor(np.ascontiguousarray(charges, dtype=np.float64), device=self.device)
+        S = torch.empty((n, n), dtype=torch.float64, device=self.device)
+        T = torch.empty_like(S)
+        V = torch.empty_like(S)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().sf_one_electron(self._h, _ptr(xyz), _ptr(Z), len(Z), _ptr(S), _ptr(T), _ptr(V),
+                                                  _stream_ptr()))
+        return S, T, V
+
+
+def _comp_factor(shell) -> float:
+    """Library factor of component (lx,ly,lz) relative to x^l (see segfock.h)."""
+    from .molecule import factorial2
+    l = sum(shell)
+    return np.sqrt(factorial2(2 * l - 1) / (factorial2(2 * shell[0] - 1) * factorial2(2 * shell[1] - 1) *
+                                            factorial2(2 * shell[2] - 1)))
+
+
+def _comp_index(shell) -> int:
+    from .molecule import CART
+    return CART[sum(shell)].index(tuple(int(v) for v in shell))
+
+
+def eri_rys(coefs1, coefs2, coefs3, coefs4, expns1, expns2, expns3, expns4, shell1, shell2, shell3, shell4,
+            normalize_factors1, normalize_factors2, normalize_factors3, normalize_factors4,
+            center1, center2, center3, center4, device="cuda") -> float:
+    """Drop-in for ``rys.eri_rys`` (core.f90:967-1002; called at hf.py:26-30):
+    one contracted Cartesian AO quartet, same 20 arguments and meaning, computed
+    by the GPU kernels.  ``shell`` beyond l = 2 raises SegFockError."""
+    args = [(coefs1, expns1, shell1, normalize_factors1, center1), (coefs2, expns2, shell2, normalize_factors2, center2),
+            (coefs3, expns3, shell3, normalize_factors3, center3), (coefs4, expns4, shell4, normalize_factors4, center4)]
+    ls, nprim, aoo, cen, exps, coefs, comp = [], [], [], [], [], [], []
+    off = 0
+    for c, e, s, nf, r in args:
+        s = [int(v) for v in s]
+        l = sum(s)
+        if l > 2:
+            raise _lib.SegFockError(-2, "eri_rys: angular momentum above d is not supported")
+        eff = np.asarray(c, dtype=np.float64) * np.asarray(nf, dtype=np.float64) / _comp_factor(s)
+        ls.append(l); nprim.append(len(eff)); aoo.append(off); cen.append(np.asarray(r, dtype=np.float64))
+        exps.append(np.asarray(e, dtype=np.float64)); coefs.append(eff); comp.append(_comp_index(s))
+        off += (l + 1) * (l + 2) // 2
+    po = np.zeros(5, dtype=np.int32)
+    po[1:] = np.cumsum(nprim)
+    table = dict(l=np.array(ls, dtype=np.int32), nprim=np.array(nprim, dtype=np.int32),
+                 atom=np.arange(4, dtype=np.int32), ao_offset=np.array(aoo, dtype=np.int32),
+                 center=np.array(cen), prim_offset=po, exps=np.concatenate(exps), coefs=np.concatenate(coefs))
+    fb = FockBuilder(table, device=device)
+    try:
+        blk = fb.eri_quartets(np.array([[0, 1, 2, 3]], dtype=np.int32))[0]
+    finally:
+        fb.close()
+    return float(blk[comp[0], comp[1], comp[2], comp[3]])

@@ -1,0 +1,216 @@
+"""GPU parity: libsegfock (through its C ABI) against the oracle and the
+reference's golden values.  Tolerances: FP64 integrals 1e-12 relative to the
+largest integral of the quartet (bit-level agreement is not expected: the
+roots, recurrences and summation order differ); FP32 integrals 2e-5 of the
+largest; energies 1e-8 Eh (FP64 path) / 1e-6 Eh (mixed path)."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import CGF, load_golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+H2O = (["O", "H", "H"], [[0, 0, 0], [0.757, 0.587, 0], [-0.757, 0.587, 0]])
+
+
+def _fb(mol, **kw):
+    from segfault_py_gb300.fock import FockBuilder
+    return FockBuilder(mol, **kw)
+
+
+def _shell_cgfs(table, s):
+    """oracle CGFs of every Cartesian component of shell s of a shell table"""
+    from segfault_py_gb300.molecule import CART
+    from segfault_py_gb300.fock import _comp_factor
+    l = int(table["l"][s])
+    o, n = int(table["prim_offset"][s]), int(table["nprim"][s])
+    out = []
+    for comp in CART[l]:
+        c = CGF(dict(coefs=list(table["coefs"][o:o + n] * _comp_factor(comp)), expns=list(table["exps"][o:o + n]),
+                     shell=list(comp), nf=[1.0] * n, center=list(table["center"][s])))
+        out.append(c)
+    return out
+
+
+def test_h2o_sto3g_all_eris(cuda, h2o_golden):
+    from segfault_py_gb300.molecule import Molecule
+    mol = Molecule.from_geometry(*H2O, "sto-3g")
+    E = _fb(mol).build_eri()
+    q = np.array(h2o_golden["quartets"])
+    got = E[q[:, 0], q[:, 1], q[:, 2], q[:, 3]]
+    assert np.abs(got - np.array(h2o_golden["eri"])).max() < 1e-13
+
+
+def test_eri_rys_shim_matches_reference(cuda, quartet_golden):
+    from segfault_py_gb300.fock import eri_rys
+    sh = quartet_golden["shells"]
+    for e in quartet_golden["quartets"][::9]:
+        cg = [sh[s]["cgfs"][c] for s, c in zip(e["shells"], e["comps"])]
+        v = eri_rys(*[g["coefs"] for g in cg], *[g["expns"] for g in cg], *[g["shell"] for g in cg],
+                    *[g["nf"] for g in cg], *[g["center"] for g in cg])
+        assert abs(v - e["value"]) <= 1e-12 * max(1.0, abs(e["value"])) + 1e-11 * abs(e["value"])
+
+
+@pytest.mark.parametrize("precision,rtol,gtol", [("fp64", 1e-10, 1e-14), ("fp32", 2e-5, 1e-7)])
+def test_all_classes_random_shells_vs_oracle(cuda, precision, rtol, gtol):
+    """Every (la,lb,lc,ld) order of l <= 2 on random contracted shells
+    (exponents up to 1e4).  Reference: the oracle with exact Rys roots.  The
+    oracle's own root variants (table / exact / reference root5) already differ
+    by up to 3e-11 of a quartet's largest integral on these shells, so the FP64
+    bound is 1e-10 of the quartet maximum plus 1e-14 of the largest integral
+    of the whole set (quartets that underflow); FP32: 2e-5 and 1e-7."""
+    from segfault_py_gb300 import geometry as G
+    table = G.random_quartet_shells(40, seed=11, kmax=4, box=4.0)
+    rng = np.random.default_rng(5)
+    ls = table["l"]
+    quartets = []
+    for la in range(3):
+        for lb in range(3):
+            for lc in range(3):
+                for ld in range(3):
+                    for _ in range(2):
+                        quartets.append([rng.choice(np.where(ls == l)[0]) for l in (la, lb, lc, ld)])
+    quartets = np.array(quartets, dtype=np.int32)
+    blocks = _fb(table).eri_quartets(quartets, precision=precision)
+    refs = []
+    O.use_exact_roots(True)
+    try:
+        for q, blk in zip(quartets, blocks):
+            cg = [_shell_cgfs(table, s) for s in q]
+            n0, n1, n2, n3 = (len(c) for c in cg)
+            idx = [[i, n0 + j, n0 + n1 + k, n0 + n1 + n2 + l]
+                   for i in range(n0) for j in range(n1) for k in range(n2) for l in range(n3)]
+            refs.append(O.eri_list(cg[0] + cg[1] + cg[2] + cg[3], np.array(idx)).reshape(blk.shape))
+    finally:
+        O.use_exact_roots(False)
+    gmax = max(np.abs(r).max() for r in refs)
+    for q, blk, ref in zip(quartets, blocks, refs):
+        bound = rtol * np.abs(ref).max() + gtol * gmax
+        assert np.abs(blk - ref).max() <= bound, (q.tolist(), np.abs(blk - ref).max(), np.abs(ref).max())
+
+
+def test_one_electron_vs_reference(cuda, h2o_golden):
+    from segfault_py_gb300.molecule import Molecule
+    mol = Molecule.from_geometry(*H2O, "sto-3g")
+    S, T, V = (m.cpu().numpy() for m in _fb(mol).one_electron())
+    for k, M in zip("STV", (S, T, V)):
+        np.testing.assert_allclose(M, np.array(h2o_golden[k]), atol=1e-12)
+
+
+def test_one_electron_d_shells_vs_oracle(cuda):
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.molecule import Molecule
+    s, x = G.water_cluster(2, seed=1)
+    mol = Molecule.from_geometry(s, x, "6-31g*")
+    S, T, V = (m.cpu().numpy() for m in _fb(mol).one_electron())
+    xyz, Z = mol.atom_table()
+    So, To, Vo = O.one_electron(mol.cgfs, xyz, Z)
+    np.testing.assert_allclose(S, So, atol=1e-12)
+    np.testing.assert_allclose(T, To, atol=1e-11)
+    np.testing.assert_allclose(V, Vo, atol=1e-10)
+
+
+def _rand_density(n, seed=0):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((n, n)) * 0.1
+    return A + A.T
+
+
+@pytest.mark.parametrize("basis", ["sto-3g", "6-31g*"])
+def test_jk_vs_oracle(cuda, basis):
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.molecule import Molecule
+    s, x = G.water_cluster(2, seed=4)
+    mol = Molecule.from_geometry(s, x, basis)
+    D = _rand_density(mol.nao)
+    fb = _fb(mol, cutoff=0.0)
+    J, K = fb.jk(torch.tensor(D, device=cuda))
+    Jo, Ko = O.jk_direct(mol.cgfs, D)
+    scale = max(np.abs(Jo).max(), np.abs(Ko).max())
+    assert np.abs(J.cpu().numpy() - Jo).max() < 1e-12 * scale
+    assert np.abs(K.cpu().numpy() - Ko).max() < 1e-12 * scale
+    # FP32 quartets: same J/K to FP32 accuracy
+    J32, K32 = fb.jk(torch.tensor(D, device=cuda), precision="fp32")
+    assert np.abs(J32.cpu().numpy() - Jo).max() < 3e-6 * scale
+    assert np.abs(K32.cpu().numpy() - Ko).max() < 3e-6 * scale
+
+
+def test_screened_quartet_count_matches_rule(cuda):
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.molecule import Molecule
+    s, x = G.water_cluster(4, seed=2)
+    mol = Molecule.from_geometry(s, x, "6-31g*")
+    fb = _fb(mol, cutoff=1e-10)
+    D = torch.tensor(_rand_density(mol.nao), device=cuda)
+    fb.jk(D, stats=True)
+    st = fb.last_stats
+    ls = fb.l
+    pairs = [(a, b) for a in range(fb.nshell) for b in range(fb.nshell)
+             if ls[a] > ls[b] or (ls[a] == ls[b] and a >= b)]
+    pc = lambda a, b: ls[a] * (ls[a] + 1) // 2 + ls[b]
+    Q = np.array([fb.q[a, b] for a, b in pairs])
+    cls = np.array([pc(a, b) for a, b in pairs])
+    n_total = n_pass = 0
+    for X in range(6):
+        for Y in range(X + 1):
+            qx, qy = Q[cls == X], Q[cls == Y]
+            if X == Y:
+                prod = np.outer(qx, qx)[np.tril_indices(len(qx))]
+            else:
+                prod = np.outer(qx, qy).ravel()
+            n_total += prod.size
+            n_pass += int(np.sum(prod >= 1e-10))
+    assert st["quartets_total"] == n_total
+    assert st["quartets_fp64"] + st["quartets_fp32"] == n_pass
+
+
+def test_scf_h2o_sto3g_energy(cuda, h2o_golden):
+    from segfault_py_gb300.molecule import Molecule
+    from segfault_py_gb300.scf import scf_diis
+    mol = Molecule.from_geometry(*H2O, "sto-3g")
+    r = scf_diis(mol, tol=1e-10)
+    assert r.converged
+    assert abs(r.energy - h2o_golden["e_rhf"]) < 1e-9
+    assert abs(r.energy - (-74.96306315472287)) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["water", "ammonia", "methane", "hydrogen_peroxide"])
+def test_scf_ccpvdz_vs_reference_recorded(cuda, name):
+    from segfault_py_gb300.molecule import Molecule
+    from segfault_py_gb300.scf import scf_diis
+    g = load_golden("ccpvdz_recorded.json")
+    m = g["molecules"][name]
+    with tempfile.TemporaryDirectory() as td:
+        bas = os.path.join(td, "cc-pvdz.dat")
+        with open(bas, "w") as f:
+            f.write("****\n" + "\n****\n".join(g["basis_blocks"].values()) + "\n****\n")
+        xyz = os.path.join(td, name + ".xyz")
+        with open(xyz, "w") as f:
+            f.write(m["xyz"])
+        mol = Molecule(xyz, bas)
+    assert mol.nao == m["recorded"]["ncgf"]
+    r = scf_diis(mol, tol=1e-10)
+    assert r.converged
+    assert abs(r.energy - m["recorded"]["etot"]) < 1e-8
+
+
+def test_mixed_precision_energy_error(cuda):
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.molecule import Molecule
+    from segfault_py_gb300.scf import scf_diis
+    s, x = G.water_cluster(8, seed=0)
+    mol = Molecule.from_geometry(s, x, "6-31g*")
+    r = scf_diis(mol, tol=1e-10)
+    fb = _fb(mol)
+    H, D = r.H, r.D
+    def energy(prec):
+        J, K = fb.jk(D, precision=prec)
+        F = H + J - 0.5 * K
+        return float(0.5 * torch.sum(D * (H + F)))
+    e64, emx = energy("fp64"), energy("mixed")
+    assert abs(emx - e64) < 1e-6

@@ -1,0 +1,122 @@
+"""Host-side logic (no GPU): basis ingestion parity, shell tables, geometry
+generators, the C ABI exports and the library's Rys root tables."""
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO, load_golden
+from oracle import oracle as O
+from segfault_py_gb300 import geometry as G
+from segfault_py_gb300.molecule import Molecule
+
+
+def test_molecule_matches_reference_cgfs(h2o_golden):
+    mol = Molecule.from_geometry(["O", "H", "H"], [[0, 0, 0], [0.757, 0.587, 0], [-0.757, 0.587, 0]], "sto-3g")
+    assert abs(mol.e_nuc - h2o_golden["e_nuc"]) < 1e-13
+    assert len(mol.cgfs) == len(h2o_golden["cgfs"]) == 7
+    for mine, ref in zip(mol.cgfs, h2o_golden["cgfs"]):
+        assert list(mine.shell) == ref["shell"]
+        np.testing.assert_allclose(mine.coefs, ref["coefs"], rtol=1e-15)
+        np.testing.assert_allclose(mine.normalize_factors, ref["nf"], rtol=1e-15)
+        np.testing.assert_allclose(mine.center, ref["center"], rtol=1e-15)
+
+
+def test_shell_table_reproduces_component_coefficients():
+    s, x = G.water_cluster(2, seed=3)
+    mol = Molecule.from_geometry(s, x, "6-31g*")
+    t = mol.shell_table()
+    from segfault_py_gb300.fock import _comp_factor
+    for sh in mol.shells:
+        for cg in sh.cgfs:
+            eff = np.asarray(cg.coefs) * cg.normalize_factors
+            np.testing.assert_allclose(sh.coefs * _comp_factor(cg.shell), eff, rtol=1e-14)
+    assert t["ao_offset"][-1] + (t["l"][-1] + 1) * (t["l"][-1] + 2) // 2 == mol.nao == 38
+
+
+def test_config_sizes():
+    for n, nao, nsh in [(8, 152, 80), (16, 304, 160)]:
+        s, x = G.water_cluster(n)
+        m = Molecule.from_geometry(s, x, "6-31g*")
+        assert (m.nao, len(m.shells)) == (nao, nsh)
+    s, x = G.alkane(20)
+    m = Molecule.from_geometry(s, x, "6-31g**")
+    assert (m.nao, len(m.shells), m.natom) == (510, 246, 62)
+
+
+def test_water_cluster_is_seeded():
+    a = G.water_cluster(8, seed=0)[1]
+    b = G.water_cluster(8, seed=0)[1]
+    c = G.water_cluster(8, seed=1)[1]
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    # monomer geometry preserved by the rotation
+    for k in range(8):
+        o, h1, h2 = a[3 * k: 3 * k + 3]
+        assert abs(np.linalg.norm(h1 - o) - np.hypot(0.757, 0.587)) < 1e-12
+        assert abs(np.linalg.norm(h2 - o) - np.hypot(0.757, 0.587)) < 1e-12
+
+
+def test_basis_not_available():
+    from segfault_py_gb300.molecule import BasisSetNotAvailableError
+    with pytest.raises(BasisSetNotAvailableError):
+        Molecule.from_geometry(["N"], [[0, 0, 0]], "sto-3g")
+
+
+def _header_symbols():
+    txt = open(f"{REPO}/include/segfock.h").read()
+    return sorted(set(re.findall(r"\b(sf_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from segfault_py_gb300 import _lib
+    L = _lib.lib()
+    syms = _header_symbols()
+    assert len(syms) >= 12
+    for s in syms:
+        assert hasattr(L, s), s
+
+
+def test_create_rejects_bad_shells_without_gpu():
+    import ctypes as C
+    from segfault_py_gb300 import _lib
+    L = _lib.lib()
+    e = np.array([1.0]); c = np.array([1.0])
+    arr = (_lib.ShellDesc * 1)()
+    arr[0].l = 3
+    arr[0].nprim = 1
+    arr[0].ao_offset = 0
+    arr[0].exps = e.ctypes.data_as(C.POINTER(C.c_double))
+    arr[0].coefs = c.ctypes.data_as(C.POINTER(C.c_double))
+    h = C.c_void_p()
+    assert L.sf_create(C.cast(arr, C.c_void_p), 1, C.byref(h)) == -2
+    assert b"l > 2" in L.sf_last_error()
+    arr[0].l = 0
+    e[0] = -1.0
+    assert L.sf_create(C.cast(arr, C.c_void_p), 1, C.byref(h)) == -1
+    assert L.sf_create(None, 0, C.byref(h)) == -1
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5])
+def test_library_root_tables_vs_oracle_exact(n):
+    from segfault_py_gb300 import _lib
+    L = _lib.lib()
+    u = np.zeros(n); w = np.zeros(n)
+    xs = np.concatenate([[0.0, 1e-12, 0.5, 63.999, 64.0, 64.001, 99.0, 1e3, 1e6], np.linspace(0.01, 70, 157)])
+    for x in xs:
+        ue, we = O.rys_roots_exact(n, x)
+        assert L.sf_rys_roots_host(n, float(x), 0, u.ctypes.data, w.ctypes.data) == 0
+        np.testing.assert_allclose(u, ue, rtol=5e-14)
+        np.testing.assert_allclose(w, we, rtol=5e-14)
+        assert L.sf_rys_roots_host(n, float(x), 1, u.ctypes.data, w.ctypes.data) == 0
+        np.testing.assert_allclose(u, ue, rtol=3e-6)
+        np.testing.assert_allclose(w, we, rtol=3e-6)
+
+
+def test_library_roots_vs_reference_root5():
+    from segfault_py_gb300 import _lib
+    L = _lib.lib()
+    g = load_golden("root5_ref.json")
+    u = np.zeros(5); w = np.zeros(5)
+    for x, res in zip(g["x"], g["res"]):
+        L.sf_rys_roots_host(5, float(x), 0, u.ctypes.data, w.ctypes.data)
+        np.testing.assert_allclose(np.concatenate([u, w]), res, rtol=2e-12)
