@@ -8,10 +8,10 @@
 // (X|Y) with pair class X >= Y, and for X == Y the ket pair index <= the bra
 // pair index.  After sf_schwarz the pairs of each class are sorted by Q
 // descending, so for bra pair i the ket pairs that pass Q_i Q_j >= cutoff are
-// a prefix of the ket list; a quartet index q maps to (i, j) through the
-// prefix sums of those prefix lengths (no explicit quartet list is stored).
-// In the mixed mode the prefix splits at Q_i Q_j >= fp32_cutoff into an FP64
-// head and an FP32 tail.
+// a prefix of the ket list (found by binary search); in the mixed mode that
+// prefix splits at Q_i Q_j >= fp32_cutoff into an FP64 head and an FP32 tail.
+// The surviving quartets of each (class, precision) are then listed
+// explicitly, ordered by primitive cost (see build_work).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -150,8 +150,7 @@ struct sf_handle {
   bool profiling = false;
   std::vector<cudaEvent_t> ev;   // 2 per slice while profiling
   std::vector<Slice> slices;
-  DBuf<int64_t> d_prefix;
-  DBuf<int> d_jstart;
+  DBuf<int2> d_list;
   double c_cut = -1, c_cut32 = -1;
   int c_prec = -1, c_part = -1, c_nparts = -1;
   int64_t st_q[2] = {0, 0}, st_pq[2] = {0, 0}, st_total = 0;
@@ -195,24 +194,32 @@ int64_t count_pass(const double *qy, int ny, double qi, double cut) {
   return e - qy;
 }
 
+// Quartet lists of every (class, precision) launch for the given cutoffs.
+// Each list holds the surviving canonical quartets (bra i, ket j) of one
+// class, ordered by decreasing primitive cost K_ab K_cd (then K_ab), stable,
+// so consecutive quartets -- the lanes and groups of one warp -- run the same
+// number of primitive iterations; inside a cost bucket the (i, j) order of the
+// Schwarz-sorted pair lists is kept.  A partition (part, nparts) keeps every
+// nparts-th quartet of each sorted list, which balances cost across parts.
 int build_work(sf_handle *h, int prec, double cut, double cut32) {
   if (h->c_prec == prec && h->c_cut == cut && h->c_cut32 == cut32 && h->c_part == h->part &&
       h->c_nparts == h->nparts)
     return SF_OK;
   h->slices.clear();
-  std::vector<int64_t> prefix;
-  std::vector<int> jstart;
+  std::vector<int2> all;
   struct Pending {
     int cls, prec;
-    size_t poff, joff;
-    int64_t total, prims;
+    size_t off;
+    int64_t n, prims;
     double flops;
-    int nX, x0, y0, same;
+    int x0, y0, same;
   };
   std::vector<Pending> pend;
   h->st_q[0] = h->st_q[1] = h->st_pq[0] = h->st_pq[1] = 0;
   h->st_f[0] = h->st_f[1] = 0.0;
   h->st_total = 0;
+  constexpr int KB = kMaxPrim * kMaxPrim + 1;   // primitive pairs per shell pair <= 256
+  std::vector<int64_t> hist((size_t)KB * KB);
   for (int cls = 0; cls < kNumClass; ++cls) {
     const ClassInfo &ci = kClassInfo[cls];
     const int X = pair_class_of(ci.la, ci.lb), Y = pair_class_of(ci.lc, ci.ld);
@@ -222,8 +229,6 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     h->st_total += same ? (int64_t)nX * (nX + 1) / 2 : (int64_t)nX * nY;
     if (nX == 0 || nY == 0) continue;
     const double *qx = h->pq.data() + x0, *qy = h->pq.data() + y0;
-    std::vector<int64_t> npy(nY + 1, 0);   // prefix of ket primitive-pair counts
-    for (int j = 0; j < nY; ++j) npy[j + 1] = npy[j] + h->pnp[y0 + j];
     std::vector<int64_t> m(nX), m64(nX);
     for (int i = 0; i < nX; ++i) {
       int64_t mi = count_pass(qy, nY, qx[i], cut);
@@ -238,53 +243,68 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     const int nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
     const double nabcd = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
     for (int pr = 0; pr < 2; ++pr) {
+      // counting sort on (K_ab, K_cd)
+      std::fill(hist.begin(), hist.end(), 0);
+      int64_t n = 0;
+      for (int i = 0; i < nX; ++i) {
+        const int64_t lo = pr == 0 ? 0 : m64[i], hi = pr == 0 ? m64[i] : m[i];
+        const int ka = h->pnp[x0 + i];
+        for (int64_t j = lo; j < hi; ++j) ++hist[(size_t)ka * KB + h->pnp[y0 + j]];
+        n += hi - lo;
+      }
+      if (n == 0) continue;
+      std::vector<int> keys;
+      for (int k = 0; k < KB * KB; ++k)
+        if (hist[k]) keys.push_back(k);
+      std::sort(keys.begin(), keys.end(), [&](int a, int b) {
+        const int ca = (a / KB) * (a % KB), cb = (b / KB) * (b % KB);
+        return ca != cb ? ca > cb : a > b;
+      });
+      std::vector<int64_t> pos((size_t)KB * KB, 0);
+      int64_t run = 0, prims = 0;
+      for (int k : keys) {
+        pos[k] = run;
+        run += hist[k];
+        prims += hist[k] * (int64_t)(k / KB) * (k % KB);
+      }
+      std::vector<int2> lst(n);
+      for (int i = 0; i < nX; ++i) {
+        const int64_t lo = pr == 0 ? 0 : m64[i], hi = pr == 0 ? m64[i] : m[i];
+        const int ka = h->pnp[x0 + i];
+        for (int64_t j = lo; j < hi; ++j) lst[pos[(size_t)ka * KB + h->pnp[y0 + j]]++] = make_int2(i, (int)j);
+      }
       Pending p;
       p.cls = cls;
       p.prec = pr;
-      p.poff = prefix.size();
-      p.joff = jstart.size();
-      p.nX = nX;
+      p.off = all.size();
       p.x0 = x0;
       p.y0 = y0;
       p.same = same;
-      int64_t run = 0, prims = 0;
-      prefix.push_back(0);
-      for (int i = 0; i < nX; ++i) {
-        const int64_t lo = pr == 0 ? 0 : m64[i], hi = pr == 0 ? m64[i] : m[i];
-        run += hi - lo;
-        prefix.push_back(run);
-        jstart.push_back((int)lo);
-        prims += (int64_t)h->pnp[x0 + i] * (npy[hi] - npy[lo]);
+      if (h->nparts > 1) {
+        int64_t kept = 0;
+        for (int64_t q = h->part; q < n; q += h->nparts) lst[kept++] = lst[q];
+        lst.resize(kept);
       }
-      p.total = run;
-      p.prims = prims;
-      p.flops = (double)prims * nr * 4.0 * nabcd + 12.0 * nabcd * (double)run;
-      h->st_q[pr] += run;
-      h->st_pq[pr] += prims;
-      h->st_f[pr] += (double)prims * nr * 4.0 * nabcd + 12.0 * nabcd * (double)run;
-      if (run > 0) pend.push_back(p);
-      else {
-        prefix.resize(p.poff);
-        jstart.resize(p.joff);
-      }
+      const double frac = (double)lst.size() / (double)n;
+      p.n = (int64_t)lst.size();
+      p.prims = (int64_t)(prims * frac);
+      p.flops = ((double)prims * nr * 4.0 * nabcd + 12.0 * nabcd * (double)n) * frac;
+      h->st_q[pr] += p.n;
+      h->st_pq[pr] += p.prims;
+      h->st_f[pr] += p.flops;
+      all.insert(all.end(), lst.begin(), lst.end());
+      if (p.n > 0) pend.push_back(p);
     }
   }
-  SF_CK(h->d_prefix.upload(prefix));
-  SF_CK(h->d_jstart.upload(jstart));
+  SF_CK(h->d_list.upload(all));
   for (const Pending &p : pend) {
     ClassWork w;
-    w.prefix = h->d_prefix.p + p.poff;
-    w.jstart = h->d_jstart.p + p.joff;
-    w.nX = p.nX;
+    w.list = h->d_list.p + p.off;
+    w.n = p.n;
     w.x0 = p.x0;
     w.y0 = p.y0;
     w.same = p.same;
-    w.q_begin = p.total * h->part / h->nparts;
-    w.q_end = p.total * (h->part + 1) / h->nparts;
-    if (w.q_end > w.q_begin) {
-      const double frac = (double)(w.q_end - w.q_begin) / (double)p.total;
-      h->slices.push_back({p.cls, p.prec, w, w.q_end - w.q_begin, (int64_t)(p.prims * frac), p.flops * frac});
-    }
+    h->slices.push_back({p.cls, p.prec, w, p.n, p.prims, p.flops});
   }
   h->c_prec = prec;
   h->c_cut = cut;
@@ -551,14 +571,13 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
   SF_CK(cudaGetLastError());
   ++launches;
   if (stats) {
-    const double frac = 1.0 / h->nparts;
-    stats->quartets_fp64 = (int64_t)(h->st_q[0] * frac);
-    stats->quartets_fp32 = (int64_t)(h->st_q[1] * frac);
+    stats->quartets_fp64 = h->st_q[0];
+    stats->quartets_fp32 = h->st_q[1];
     stats->quartets_total = h->st_total;
-    stats->prim_quartets_fp64 = (int64_t)(h->st_pq[0] * frac);
-    stats->prim_quartets_fp32 = (int64_t)(h->st_pq[1] * frac);
-    stats->flop_alg_fp64 = h->st_f[0] * frac;
-    stats->flop_alg_fp32 = h->st_f[1] * frac;
+    stats->prim_quartets_fp64 = h->st_pq[0];
+    stats->prim_quartets_fp32 = h->st_pq[1];
+    stats->flop_alg_fp64 = h->st_f[0];
+    stats->flop_alg_fp32 = h->st_f[1];
     stats->launches = launches;
     stats->reserved = 0;
     SF_CK(cudaStreamSynchronize(st));

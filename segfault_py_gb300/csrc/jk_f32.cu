@@ -7,7 +7,7 @@ namespace sf {
 template <int LA, int LB, int LC, int LD, int T>
 static cudaError_t run_jk32(const KParams &kp, const ClassWork &w, const float *D, double *Jh, double *Kh,
                             cudaStream_t st) {
-  const int64_t n = w.q_end - w.q_begin;
+  const int64_t n = w.n;
   if (n <= 0) return cudaSuccess;
   constexpr int G = kBlock / T;
   constexpr size_t smem = grp_smem<LA, LB, LC, LD, float, T>();

@@ -526,28 +526,16 @@ __device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
 }
 
 // ---------------------------------------------------------------------------
-// work description of one (class, precision) slice of the implicit quartet
-// list: for bra pair i (class X, sorted by Q), the ket pairs are j in
-// [jstart[i], jstart[i] + prefix[i+1] - prefix[i]) of class Y.
+// work description of one (class, precision) launch: an explicit list of
+// (bra pair index in class X, ket pair index in class Y), sorted on the host
+// by primitive cost so that the lanes / groups of a warp run identical loops
 // ---------------------------------------------------------------------------
 struct ClassWork {
-  const int64_t *prefix;   // nX + 1
-  const int *jstart;       // nX, or null (= 0)
-  int64_t q_begin, q_end;  // slice of [0, prefix[nX])
-  int nX;
+  const int2 *list;
+  int64_t n;
   int x0, y0;              // first global pair index of class X / Y
   int same;                // X == Y
 };
-
-__device__ __forceinline__ void decode_quartet(const ClassWork &w, int64_t q, int &i, int &j) {
-  int lo = 0, hi = w.nX;   // prefix[lo] <= q < prefix[hi]
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(w.prefix + mid) <= q) lo = mid; else hi = mid;
-  }
-  i = lo;
-  j = (w.jstart ? __ldg(w.jstart + lo) : 0) + (int)(q - __ldg(w.prefix + lo));
-}
 
 constexpr int kBlock = 128;
 
@@ -556,10 +544,10 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
                                                     double *Kh) {
   constexpr int G = kBlock / T;
   const int grp = threadIdx.x / T, t = threadIdx.x % T;
-  const int64_t q = w.q_begin + (int64_t)blockIdx.x * G + grp;
-  if (q >= w.q_end) return;
-  int i, j;
-  decode_quartet(w, q, i, j);
+  const int64_t q = (int64_t)blockIdx.x * G + grp;
+  if (q >= w.n) return;
+  const int2 ij = __ldg(w.list + q);
+  const int i = ij.x, j = ij.y;
   const int pab = w.x0 + i, pcd = w.y0 + j;
   const QGeom<R> g = make_geom<R>(kp, pab, pcd, false, false);
   double scale = 1.0;

@@ -38,7 +38,22 @@ class SCFResult:
     history: list = field(default_factory=list, repr=False)
 
 
+def preload_torch_linalg():
+    """Load torch's CUDA linear-algebra library by absolute path.  torch opens
+    it lazily by bare name on the first GPU eigh/solve; under a profiler that
+    injects itself into the process that lookup can fail."""
+    import ctypes
+    import os
+    p = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
+    if os.path.exists(p):
+        try:
+            ctypes.CDLL(p, mode=ctypes.RTLD_GLOBAL)
+        except OSError:
+            pass
+
+
 def _setup(mol: Molecule, fb: FockBuilder | None, precision, cutoff, fp32_cutoff, device):
+    preload_torch_linalg()
     if fb is None:
         fb = FockBuilder(mol, device=device, cutoff=cutoff, fp32_cutoff=fp32_cutoff, precision=precision)
     S, T, V = fb.one_electron()
