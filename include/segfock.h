@@ -168,6 +168,31 @@ int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out);
  * reference.  Synchronises the stream. */
 int sf_fma_peak(int32_t precision, double *flops, float *ms, void *stream);
 
+/* Allocation-free Fock build.  No counterpart in the reference.
+ *
+ * Same result and arguments as sf_fock_jk (without stats), for callers that
+ * cannot call cudaMalloc when they build a Fock matrix: code that runs where
+ * another component owns all device memory (a framework's memory pool, a
+ * fixed memory budget) or a time-critical loop that must not enter the CUDA
+ * allocator.  The scratch sf_fock_jk keeps in the handle (the half matrices
+ * Jh, Kh and the single-precision copy of D) lives here in one static device
+ * array of the library, sized for nao <= SF_NOALLOC_MAX_NAO (2.5 * 1024^2
+ * doubles = 20 MiB, held on every GPU that loads the library until the
+ * process exits).  Larger handles are rejected with SF_EINVAL.
+ *
+ * The call allocates nothing: no cudaMalloc, cudaFree or allocating library
+ * routine.  Set-up that does allocate must happen before it: sf_create,
+ * sf_schwarz, and one sf_fock_jk call with the same precision and cutoffs,
+ * which builds the quartet lists of the handle (otherwise SF_ESTATE).  The
+ * first call on a device looks up the device address of the static array
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  Every call shares the one array: calls that overlap on
+ * the GPU (other streams, other threads, other handles) race and must be
+ * serialised by the caller.  The array is cleared by each call before use. */
+#define SF_NOALLOC_MAX_NAO 1024
+int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int32_t precision,
+                       double cutoff, double fp32_cutoff, void *stream);
+
 /* Host evaluation of the library's Rys root table (for checks without a GPU):
  * n-point rule at x, u[i] = t_i^2, w[i] weights; fp32 != 0 selects the
  * single-precision table. */

@@ -316,6 +316,18 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
 
 }  // namespace
 
+// Scratch of sf_fock_jk_noalloc: Jh and Kh (nao^2 doubles each) followed by
+// the single-precision copy of D (nao^2 floats), for nao <= SF_NOALLOC_MAX_NAO.
+static constexpr size_t kNoAllocNN = (size_t)SF_NOALLOC_MAX_NAO * SF_NOALLOC_MAX_NAO;
+static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocNN + (kNoAllocNN + 1) / 2];
+
+namespace {
+// device address of g_noalloc_scratch per device (host code cannot use the
+// symbol itself as a device pointer)
+std::mutex g_noalloc_mu;
+double *g_noalloc_dev[128] = {nullptr};
+}  // namespace
+
 extern "C" {
 
 int sf_version(void) { return 100; }
@@ -582,6 +594,54 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
     stats->reserved = 0;
     SF_CK(cudaStreamSynchronize(st));
   }
+  return SF_OK;
+}
+
+int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int32_t precision, double cutoff,
+                       double fp32_cutoff, void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_fock_jk_noalloc: NULL handle");
+  if (!D || !J || !K) return fail(SF_EINVAL, "sf_fock_jk_noalloc: NULL matrix");
+  if (precision < SF_PREC_FP64 || precision > SF_PREC_MIXED) return fail(SF_EINVAL, "sf_fock_jk_noalloc: bad precision");
+  if (h->nao > SF_NOALLOC_MAX_NAO)
+    return fail(SF_EINVAL, "sf_fock_jk_noalloc: nao = " + std::to_string(h->nao) +
+                               " exceeds the static scratch limit SF_NOALLOC_MAX_NAO = " +
+                               std::to_string(SF_NOALLOC_MAX_NAO) + "; use sf_fock_jk");
+  if (!h->have_schwarz) return fail(SF_ESTATE, "sf_fock_jk_noalloc: call sf_schwarz first");
+  if (!(h->c_prec == precision && h->c_cut == cutoff && h->c_cut32 == fp32_cutoff && h->c_part == h->part &&
+        h->c_nparts == h->nparts))
+    return fail(SF_ESTATE,
+                "sf_fock_jk_noalloc: the quartet lists for this precision and these cutoffs are not built; "
+                "call sf_fock_jk once with the same arguments first (that call allocates)");
+  DeviceGuard g(h->device);
+  if (h->device < 0 || h->device >= 128) return fail(SF_EINVAL, "sf_fock_jk_noalloc: device index out of range");
+  double *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_dev[h->device]) {
+      void *p = nullptr;
+      SF_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      g_noalloc_dev[h->device] = static_cast<double *>(p);
+    }
+    scratch = g_noalloc_dev[h->device];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n = h->nao;
+  const size_t nn = (size_t)n * n;
+  double *Jh = scratch, *Kh = scratch + nn;
+  float *D32 = reinterpret_cast<float *>(scratch + 2 * nn);
+  SF_CK(cudaMemsetAsync(scratch, 0, 2 * nn * sizeof(double), st));
+  bool need32 = false;
+  for (const auto &s : h->slices) need32 |= s.prec == 1;
+  if (need32) {
+    to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, D32, (int64_t)nn);
+    SF_CK(cudaGetLastError());
+  }
+  for (const auto &s : h->slices) {
+    if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, Jh, Kh, st));
+    else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, D32, Jh, Kh, st));
+  }
+  symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(Jh, Kh, J, K, n);
+  SF_CK(cudaGetLastError());
   return SF_OK;
 }
 
