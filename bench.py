@@ -1,7 +1,7 @@
 """Benchmark: Fock builds/s of the GPU direct-SCF J/K build.
 
 Workload (N=1): seeded (H2O)_8 water cluster, 6-31G* (Cartesian d), 152 AOs,
-80 shells; Schwarz cutoff 1e-12; FP32 cutoff 1e-5 for the mixed path.  The
+80 shells; Schwarz cutoff 1e-12; FP32 cutoff 1e-2 for the mixed path.  The
 density is the converged FP64 RHF density of that cluster (computed once,
 outside the timed region).  One step = one Fock build J, K = jk(D) (the two
 einsums of the reference's hf.py:300 without the N^4 tensor), mixed precision.
@@ -38,9 +38,9 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-METRIC = "Fock builds/s ((H2O)8 6-31G*, mixed FP32/FP64, Schwarz 1e-12)"
+METRIC = "Fock builds/s ((H2O)8 6-31G*, mixed FP32/FP64, Schwarz 1e-12, FP32 below Q_abQ_cd 1e-2)"
 CUTOFF = 1e-12
-FP32_CUTOFF = 1e-5
+FP32_CUTOFF = 1e-2
 L2_FLUSH_BYTES = 256 << 20
 
 

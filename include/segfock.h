@@ -155,7 +155,7 @@ typedef struct {
     int64_t prim_quartets;
     double flop_alg;
     float ms;                 /* device time of the last profiled launch      */
-    int32_t threads_per_quartet;
+    int32_t threads_per_quartet;   /* lanes per quartet: Cartesian split x primitive split */
 } sf_slice_info;
 
 int sf_set_profiling(sf_handle *h, int32_t on);

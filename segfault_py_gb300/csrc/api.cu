@@ -149,6 +149,13 @@ struct sf_handle {
   };
   bool profiling = false;
   std::vector<cudaEvent_t> ev;   // 2 per slice while profiling
+  // side streams: the class launches of one build are independent (they only
+  // add into Jh/Kh with atomics), so they are spread over kSideStreams
+  // streams forked from and joined back into the caller's stream
+  static constexpr int kSideStreams = 8;
+  cudaStream_t side[kSideStreams] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kSideStreams] = {};
+  std::vector<int> slice_stream;   // side stream of each slice (greedy by cost)
   std::vector<Slice> slices;
   DBuf<int2> d_list;
   double c_cut = -1, c_cut32 = -1;
@@ -213,6 +220,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     int64_t n, prims;
     double flops;
     int x0, y0, same;
+    int psplit;
   };
   std::vector<Pending> pend;
   h->st_q[0] = h->st_q[1] = h->st_pq[0] = h->st_pq[1] = 0;
@@ -274,6 +282,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
         for (int64_t j = lo; j < hi; ++j) lst[pos[(size_t)ka * KB + h->pnp[y0 + j]]++] = make_int2(i, (int)j);
       }
       Pending p;
+      p.psplit = 1;
       p.cls = cls;
       p.prec = pr;
       p.off = all.size();
@@ -292,8 +301,35 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       h->st_q[pr] += p.n;
       h->st_pq[pr] += p.prims;
       h->st_f[pr] += p.flops;
+      // split the cost-sorted list into launches with P primitive sub-groups
+      // per quartet: heavy quartets (many primitive quartets) get more lanes
+      const int T = pr == 0 ? ci.t64 : ci.t32;
+      const int pmax = 32 / T;
+      auto psplit = [&](int64_t cost) {
+        if (pmax > 1 && cost >= 4 * pmax) return pmax;
+        if (pmax > 8 && cost >= 32) return 8;
+        return 1;
+      };
+      int64_t q0 = 0;
+      while (q0 < p.n) {
+        const auto cost_of = [&](int64_t q) {
+          return (int64_t)h->pnp[x0 + lst[q].x] * h->pnp[y0 + lst[q].y];
+        };
+        const int P = psplit(cost_of(q0));
+        int64_t q1 = q0 + 1;
+        while (q1 < p.n && psplit(cost_of(q1)) == P) ++q1;
+        Pending seg = p;
+        seg.off = all.size() + q0;
+        seg.n = q1 - q0;
+        int64_t sp = 0;
+        for (int64_t q = q0; q < q1; ++q) sp += cost_of(q);
+        seg.prims = sp;
+        seg.flops = (double)sp * nr * 4.0 * nabcd + 12.0 * nabcd * (double)seg.n;
+        seg.psplit = P;
+        pend.push_back(seg);
+        q0 = q1;
+      }
       all.insert(all.end(), lst.begin(), lst.end());
-      if (p.n > 0) pend.push_back(p);
     }
   }
   SF_CK(h->d_list.upload(all));
@@ -304,13 +340,70 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     w.x0 = p.x0;
     w.y0 = p.y0;
     w.same = p.same;
+    w.psplit = p.psplit;
     h->slices.push_back({p.cls, p.prec, w, p.n, p.prims, p.flops});
+  }
+  // greedy longest-processing-time assignment of slices to side streams;
+  // cost estimate: primitive quartets x roots x Cartesian outputs, FP64 work
+  // weighted by the FP64:FP32 throughput ratio of the part
+  {
+    std::vector<int> order(h->slices.size());
+    std::vector<double> cost(h->slices.size());
+    for (size_t k = 0; k < h->slices.size(); ++k) {
+      const auto &sl = h->slices[k];
+      const ClassInfo &ci = kClassInfo[sl.cls];
+      const double nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
+      const double nc = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
+      cost[k] = (double)sl.prims * (nr * (nc + 30.0) + 40.0) * (sl.prec == 0 ? 16.0 : 1.0);
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<sf_handle::Slice> sorted;
+    for (int k : order) sorted.push_back(h->slices[k]);
+    h->slices.swap(sorted);
+    std::sort(cost.begin(), cost.end(), std::greater<double>());
+    double load[sf_handle::kSideStreams] = {0};
+    h->slice_stream.assign(h->slices.size(), 0);
+    for (size_t k = 0; k < h->slices.size(); ++k) {
+      int best = 0;
+      for (int j = 1; j < sf_handle::kSideStreams; ++j)
+        if (load[j] < load[best]) best = j;
+      h->slice_stream[k] = best;
+      load[best] += cost[k];
+    }
   }
   h->c_prec = prec;
   h->c_cut = cut;
   h->c_cut32 = cut32;
   h->c_part = h->part;
   h->c_nparts = h->nparts;
+  return SF_OK;
+}
+
+// Launch every slice of the current quartet lists on the side streams
+// (forked from st, joined back into st).  Events of the profiling mode
+// bracket each launch on its own stream.
+int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, double *Kh, cudaStream_t st,
+                  bool profiling, int *launches) {
+  SF_CK(cudaEventRecord(h->fork_ev, st));
+  bool used[sf_handle::kSideStreams] = {false};
+  for (size_t k = 0; k < h->slices.size(); ++k) used[h->slice_stream[k]] = true;
+  for (int j = 0; j < sf_handle::kSideStreams; ++j)
+    if (used[j]) SF_CK(cudaStreamWaitEvent(h->side[j], h->fork_ev, 0));
+  for (size_t k = 0; k < h->slices.size(); ++k) {
+    const auto &s = h->slices[k];
+    cudaStream_t ss = h->side[h->slice_stream[k]];
+    if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k], ss));
+    if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, Jh, Kh, ss));
+    else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, D32, Jh, Kh, ss));
+    if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k + 1], ss));
+    if (launches) ++*launches;
+  }
+  for (int j = 0; j < sf_handle::kSideStreams; ++j)
+    if (used[j]) {
+      SF_CK(cudaEventRecord(h->join_ev[j], h->side[j]));
+      SF_CK(cudaStreamWaitEvent(st, h->join_ev[j], 0));
+    }
   return SF_OK;
 }
 
@@ -435,6 +528,11 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   SF_CK(cudaMemset(h->d_err.p, 0, 4 * sizeof(int)));
   int rc = upload_pairs(h);
   if (rc) return rc;
+  for (int k = 0; k < sf_handle::kSideStreams; ++k) {
+    SF_CK(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking));
+    SF_CK(cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming));
+  }
+  SF_CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
   SF_CK(prepare_jk_f64());
   SF_CK(prepare_jk_f32());
   SF_CK(prepare_eri());
@@ -451,6 +549,11 @@ void sf_destroy(sf_handle *h) {
   if (!h) return;
   DeviceGuard g(h->device);
   for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
+  for (int k = 0; k < sf_handle::kSideStreams; ++k) {
+    if (h->side[k]) cudaStreamDestroy(h->side[k]);
+    if (h->join_ev[k]) cudaEventDestroy(h->join_ev[k]);
+  }
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   delete h;
 }
 
@@ -473,7 +576,7 @@ int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out) {
   out->quartets = s.quartets;
   out->prim_quartets = s.prims;
   out->flop_alg = s.flops;
-  out->threads_per_quartet = s.prec == 0 ? ci.t64 : ci.t32;
+  out->threads_per_quartet = (s.prec == 0 ? ci.t64 : ci.t32) * s.w.psplit;
   out->ms = -1.0f;
   if (h->profiling && h->ev.size() >= 2 * h->slices.size()) {
     SF_CK(cudaEventSynchronize(h->ev[2 * idx + 1]));
@@ -571,14 +674,8 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
       h->ev.push_back(e);
     }
   }
-  for (size_t k = 0; k < h->slices.size(); ++k) {
-    const auto &s = h->slices[k];
-    if (h->profiling) SF_CK(cudaEventRecord(h->ev[2 * k], st));
-    if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, h->d_Jh.p, h->d_Kh.p, st));
-    else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st));
-    if (h->profiling) SF_CK(cudaEventRecord(h->ev[2 * k + 1], st));
-    ++launches;
-  }
+  rc = launch_slices(h, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st, h->profiling, &launches);
+  if (rc) return rc;
   symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(h->d_Jh.p, h->d_Kh.p, J, K, n);
   SF_CK(cudaGetLastError());
   ++launches;
@@ -636,10 +733,8 @@ int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int3
     to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, D32, (int64_t)nn);
     SF_CK(cudaGetLastError());
   }
-  for (const auto &s : h->slices) {
-    if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, Jh, Kh, st));
-    else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, D32, Jh, Kh, st));
-  }
+  int rc = launch_slices(h, D, D32, Jh, Kh, st, false, nullptr);
+  if (rc) return rc;
   symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(Jh, Kh, J, K, n);
   SF_CK(cudaGetLastError());
   return SF_OK;

@@ -276,34 +276,40 @@ __device__ __forceinline__ void load_prim_cd(const KParams &kp, const QGeom<R> &
 // T == 1: whole quartet in registers; acc[o] unnormalised
 // ---------------------------------------------------------------------------
 template <int LA, int LB, int LC, int LD, typename R>
-__device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R (&acc)[QC<LA, LB, LC, LD>::NABCD]) {
+__device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R (&acc)[QC<LA, LB, LC, LD>::NABCD],
+                                        int p = 0, int P = 1) {
   using Q = QC<LA, LB, LC, LD>;
   constexpr int NR = Q::NR, SZ = Q::SZ;
 #pragma unroll
   for (int o = 0; o < Q::NABCD; ++o) acc[o] = (R)0;
-  for (int ip = 0; ip < g.ab_n; ++ip) {
-    PQ<R> s;
-    R p, px, py, pz, kab;
-    load_prim_ab<R>(kp, g, ip, s, p, px, py, pz, kab);
-    for (int iq = 0; iq < g.cd_n; ++iq) {
-      load_prim_cd<R>(kp, g, iq, s, p, px, py, pz, kab);
-      R u[NR], w[NR];
-      rys_roots_all<NR, R>(kp, s.x, u, w);
+  const int nprim = g.ab_n * g.cd_n;
+  int cur = -1;
+  PQ<R> s;
+  R pp, px, py, pz, kab;
+  // primitive quartets idx = p, p+P, ... of the ab-major flattened loop
+  for (int idx = p; idx < nprim; idx += P) {
+    const int ip = idx / g.cd_n, iq = idx - ip * g.cd_n;
+    if (ip != cur) {
+      load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
+      cur = ip;
+    }
+    load_prim_cd<R>(kp, g, iq, s, pp, px, py, pz, kab);
+    R u[NR], w[NR];
+    rys_roots_all<NR, R>(kp, s.x, u, w);
 #pragma unroll
-      for (int r = 0; r < NR; ++r) {
-        const R uu = u[r];
-        const R b00 = (R)0.5 * s.r2 * uu;
-        const R b10 = s.i2p * ((R)1 - s.aq * uu);
-        const R b01 = s.i2q * ((R)1 - s.ap * uu);
-        const R tq = s.aq * uu, tp = s.ap * uu;
-        R Ix[SZ], Iy[SZ], Iz[SZ];
-        rys_2d<LA, LB, LC, LD, R>((R)1, s.pax - tq * s.pqx, s.qcx + tp * s.pqx, b00, b10, b01, g.ABx, g.CDx, Ix);
-        rys_2d<LA, LB, LC, LD, R>((R)1, s.pay - tq * s.pqy, s.qcy + tp * s.pqy, b00, b10, b01, g.ABy, g.CDy, Iy);
-        rys_2d<LA, LB, LC, LD, R>(s.pref * w[r], s.paz - tq * s.pqz, s.qcz + tp * s.pqz, b00, b10, b01, g.ABz,
-                                  g.CDz, Iz);
+    for (int r = 0; r < NR; ++r) {
+      const R uu = u[r];
+      const R b00 = (R)0.5 * s.r2 * uu;
+      const R b10 = s.i2p * ((R)1 - s.aq * uu);
+      const R b01 = s.i2q * ((R)1 - s.ap * uu);
+      const R tq = s.aq * uu, tp = s.ap * uu;
+      R Ix[SZ], Iy[SZ], Iz[SZ];
+      rys_2d<LA, LB, LC, LD, R>((R)1, s.pax - tq * s.pqx, s.qcx + tp * s.pqx, b00, b10, b01, g.ABx, g.CDx, Ix);
+      rys_2d<LA, LB, LC, LD, R>((R)1, s.pay - tq * s.pqy, s.qcy + tp * s.pqy, b00, b10, b01, g.ABy, g.CDy, Iy);
+      rys_2d<LA, LB, LC, LD, R>(s.pref * w[r], s.paz - tq * s.pqz, s.qcz + tp * s.pqz, b00, b10, b01, g.ABz,
+                                g.CDz, Iz);
 #pragma unroll
-        for (int o = 0; o < Q::NABCD; ++o) acc[o] += Ix[Q::toff(o, 0)] * Iy[Q::toff(o, 1)] * Iz[Q::toff(o, 2)];
-      }
+      for (int o = 0; o < Q::NABCD; ++o) acc[o] += Ix[Q::toff(o, 0)] * Iy[Q::toff(o, 1)] * Iz[Q::toff(o, 2)];
     }
   }
 }
@@ -321,7 +327,7 @@ struct Grp {
 
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R *tab, int t, unsigned gmask,
-                                         R (&acc)[Grp<LA, LB, LC, LD, R, T>::NPER]) {
+                                         R (&acc)[Grp<LA, LB, LC, LD, R, T>::NPER], int p = 0, int P = 1) {
   using Q = QC<LA, LB, LC, LD>;
   using GP = Grp<LA, LB, LC, LD, R, T>;
   constexpr int NR = Q::NR, SZ = Q::SZ, NPER = GP::NPER;
@@ -334,45 +340,58 @@ __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R
                              ((2 * NR * SZ + Q::toff(o, 2)) << 20))
                           : 0;
   }
-  for (int ip = 0; ip < g.ab_n; ++ip) {
-    PQ<R> s;
-    R p, px, py, pz, kab;
-    load_prim_ab<R>(kp, g, ip, s, p, px, py, pz, kab);
-    for (int iq = 0; iq < g.cd_n; ++iq) {
-      load_prim_cd<R>(kp, g, iq, s, p, px, py, pz, kab);
-      for (int task = t; task < 3 * NR; task += T) {
-        const int r = task % NR, d = task / NR;
-        R uu, ww;
-        rys_root_one<NR, R>(kp, s.x, r, uu, ww);
-        const R b00 = (R)0.5 * s.r2 * uu;
-        const R b10 = s.i2p * ((R)1 - s.aq * uu);
-        const R b01 = s.i2q * ((R)1 - s.ap * uu);
-        const R tq = s.aq * uu, tp = s.ap * uu;
-        const R pa = d == 0 ? s.pax : d == 1 ? s.pay : s.paz;
-        const R qc = d == 0 ? s.qcx : d == 1 ? s.qcy : s.qcz;
-        const R pq = d == 0 ? s.pqx : d == 1 ? s.pqy : s.pqz;
-        const R ab = d == 0 ? g.ABx : d == 1 ? g.ABy : g.ABz;
-        const R cd = d == 0 ? g.CDx : d == 1 ? g.CDy : g.CDz;
-        const R g0 = d == 2 ? s.pref * ww : (R)1;
-        R I[SZ];
-        rys_2d<LA, LB, LC, LD, R>(g0, pa - tq * pq, qc + tp * pq, b00, b10, b01, ab, cd, I);
-        R *dst = tab + (d * NR + r) * SZ;
-#pragma unroll
-        for (int i = 0; i < SZ; ++i) dst[i] = I[i];
-      }
-      __syncwarp(gmask);
-#pragma unroll
-      for (int k = 0; k < NPER; ++k) {
-        if (t + k * T < Q::NABCD) {
-          const int ox = off[k] & 1023, oy = (off[k] >> 10) & 1023, oz = off[k] >> 20;
-          R v = (R)0;
-#pragma unroll
-          for (int r = 0; r < NR; ++r) v += tab[ox + r * SZ] * tab[oy + r * SZ] * tab[oz + r * SZ];
-          acc[k] += v;
-        }
-      }
-      __syncwarp(gmask);
+  const int nprim = g.ab_n * g.cd_n;
+  int cur = -1;
+  PQ<R> s;
+  R pp, px, py, pz, kab;
+  for (int idx = p; idx < nprim; idx += P) {
+    const int ip = idx / g.cd_n, iq = idx - ip * g.cd_n;
+    if (ip != cur) {
+      load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
+      cur = ip;
     }
+    load_prim_cd<R>(kp, g, iq, s, pp, px, py, pz, kab);
+    for (int task = t; task < 3 * NR; task += T) {
+      const int r = task % NR, d = task / NR;
+      R uu, ww;
+      rys_root_one<NR, R>(kp, s.x, r, uu, ww);
+      const R b00 = (R)0.5 * s.r2 * uu;
+      const R b10 = s.i2p * ((R)1 - s.aq * uu);
+      const R b01 = s.i2q * ((R)1 - s.ap * uu);
+      const R tq = s.aq * uu, tp = s.ap * uu;
+      const R pa = d == 0 ? s.pax : d == 1 ? s.pay : s.paz;
+      const R qc = d == 0 ? s.qcx : d == 1 ? s.qcy : s.qcz;
+      const R pq = d == 0 ? s.pqx : d == 1 ? s.pqy : s.pqz;
+      const R ab = d == 0 ? g.ABx : d == 1 ? g.ABy : g.ABz;
+      const R cd = d == 0 ? g.CDx : d == 1 ? g.CDy : g.CDz;
+      const R g0 = d == 2 ? s.pref * ww : (R)1;
+      R I[SZ];
+      rys_2d<LA, LB, LC, LD, R>(g0, pa - tq * pq, qc + tp * pq, b00, b10, b01, ab, cd, I);
+      R *dst = tab + (d * NR + r) * SZ;
+#pragma unroll
+      for (int i = 0; i < SZ; ++i) dst[i] = I[i];
+    }
+    __syncwarp(gmask);
+#pragma unroll
+    for (int k = 0; k < NPER; ++k) {
+      if (t + k * T < Q::NABCD) {
+        const int ox = off[k] & 1023, oy = (off[k] >> 10) & 1023, oz = off[k] >> 20;
+        R v = (R)0;
+#pragma unroll
+        for (int r = 0; r < NR; ++r) v += tab[ox + r * SZ] * tab[oy + r * SZ] * tab[oz + r * SZ];
+        acc[k] += v;
+      }
+    }
+    __syncwarp(gmask);
+  }
+}
+
+// sum acc over the P primitive sub-groups of a quartet (lanes T apart)
+template <typename R, int N, int T>
+__device__ __forceinline__ void reduce_psplit(R (&acc)[N], int P, unsigned qmask) {
+  for (int sft = T; sft < T * P; sft <<= 1) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc[k] += __shfl_xor_sync(qmask, acc[k], sft);
   }
 }
 
@@ -535,6 +554,7 @@ struct ClassWork {
   int64_t n;
   int x0, y0;              // first global pair index of class X / Y
   int same;                // X == Y
+  int psplit;              // P: primitive sub-groups per quartet (T*P <= 32)
 };
 
 constexpr int kBlock = 128;
@@ -542,9 +562,10 @@ constexpr int kBlock = 128;
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, const R *__restrict__ D, double *Jh,
                                                     double *Kh) {
-  constexpr int G = kBlock / T;
-  const int grp = threadIdx.x / T, t = threadIdx.x % T;
-  const int64_t q = (int64_t)blockIdx.x * G + grp;
+  const int P = w.psplit;
+  const int TP = T * P;
+  const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
+  const int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp;
   if (q >= w.n) return;
   const int2 ij = __ldg(w.list + q);
   const int i = ij.x, j = ij.y;
@@ -554,18 +575,22 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
   if (g.a == g.b) scale *= 0.5;
   if (g.c == g.d) scale *= 0.5;
   if (w.same && i == j) scale *= 0.5;
+  const int lane = threadIdx.x & 31;
+  const unsigned qmask = (TP == 32) ? 0xffffffffu : (((1u << TP) - 1u) << (lane & ~(TP - 1)));
   if constexpr (T == 1) {
     R acc[QC<LA, LB, LC, LD>::NABCD];
-    eval_t1<LA, LB, LC, LD, R>(kp, g, acc);
-    digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh);
+    eval_t1<LA, LB, LC, LD, R>(kp, g, acc, p, P);
+    if (P > 1) reduce_psplit<R, QC<LA, LB, LC, LD>::NABCD, 1>(acc, P, qmask);
+    if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh);
   } else {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using GP = Grp<LA, LB, LC, LD, R, T>;
-    R *buf = reinterpret_cast<R *>(smem_raw) + grp * GP::BUFN;
-    const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1)));
+    R *buf = reinterpret_cast<R *>(smem_raw) + (threadIdx.x / T) * GP::BUFN;
+    const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
     R acc[GP::NPER];
-    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc);
-    digest_grp<LA, LB, LC, LD, R, T>(kp, g, acc, buf, t, gmask, scale, D, Jh, Kh);
+    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc, p, P);
+    if (P > 1) reduce_psplit<R, GP::NPER, T>(acc, P, qmask);
+    if (p == 0) digest_grp<LA, LB, LC, LD, R, T>(kp, g, acc, buf, t, gmask, scale, D, Jh, Kh);
   }
 }
 

@@ -11,6 +11,8 @@ Convergence is |E_n - E_{n-1}| <= tol, as in the reference.  The difference is
 the Fock build: ERIs are never stored; every iteration calls the GPU J/K
 builder (FockBuilder.jk), and S, T, V come from the GPU one-electron kernel.
 Everything stays on the device in FP64 (eigh, DIIS, energies).
+``precision`` ('fp64', 'fp32', 'mixed'), ``cutoff`` and ``fp32_cutoff``
+default to the FockBuilder's settings (fp64, 1e-12, 1e-5 for a new one).
 """
 from __future__ import annotations
 
@@ -55,7 +57,9 @@ def preload_torch_linalg():
 def _setup(mol: Molecule, fb: FockBuilder | None, precision, cutoff, fp32_cutoff, device):
     preload_torch_linalg()
     if fb is None:
-        fb = FockBuilder(mol, device=device, cutoff=cutoff, fp32_cutoff=fp32_cutoff, precision=precision)
+        fb = FockBuilder(mol, device=device, cutoff=DEFAULT_CUTOFF if cutoff is None else cutoff,
+                         fp32_cutoff=DEFAULT_FP32_CUTOFF if fp32_cutoff is None else fp32_cutoff,
+                         precision=precision or "fp64")
     S, T, V = fb.one_electron()
     H = T + V
     vals, vecs = torch.linalg.eigh(S)
@@ -86,7 +90,7 @@ def _run(mol, mode, tol, maxiter, precision, cutoff, fp32_cutoff, fb, device, da
             P_old = P_new
         else:
             P = P_new
-        J, K = fb.jk(P)
+        J, K = fb.jk(P, precision=precision, cutoff=cutoff, fp32_cutoff=fp32_cutoff)
         F = H + J - 0.5 * K
         etot = float(0.5 * torch.sum(P * (H + F)))
         hist.append(etot + mol.e_nuc)
@@ -124,19 +128,19 @@ def _run(mol, mode, tol, maxiter, precision, cutoff, fp32_cutoff, fb, device, da
                      D=P, F=F, C=C, eps=eps, H=H, S=S, history=hist)
 
 
-def scf(mol: Molecule, tol=1e-8, maxiter=30, precision="fp64", cutoff=DEFAULT_CUTOFF,
-        fp32_cutoff=DEFAULT_FP32_CUTOFF, fb=None, device="cuda") -> SCFResult:
+def scf(mol: Molecule, tol=1e-8, maxiter=30, precision=None, cutoff=None,
+        fp32_cutoff=None, fb=None, device="cuda") -> SCFResult:
     """hf.py:66-160 (no convergence acceleration)."""
     return _run(mol, "plain", tol, maxiter, precision, cutoff, fp32_cutoff, fb, device)
 
 
-def scf_damping(mol: Molecule, tol=1e-8, maxiter=100, precision="fp64", cutoff=DEFAULT_CUTOFF,
-                fp32_cutoff=DEFAULT_FP32_CUTOFF, fb=None, device="cuda") -> SCFResult:
+def scf_damping(mol: Molecule, tol=1e-8, maxiter=100, precision=None, cutoff=None,
+                fp32_cutoff=None, fb=None, device="cuda") -> SCFResult:
     """hf.py:165-232 (one old density mixed in with damping 0.1)."""
     return _run(mol, "damping", tol, maxiter, precision, cutoff, fp32_cutoff, fb, device)
 
 
-def scf_diis(mol: Molecule, tol=1e-8, maxiter=100, precision="fp64", cutoff=DEFAULT_CUTOFF,
-             fp32_cutoff=DEFAULT_FP32_CUTOFF, fb=None, device="cuda") -> SCFResult:
+def scf_diis(mol: Molecule, tol=1e-8, maxiter=100, precision=None, cutoff=None,
+             fp32_cutoff=None, fb=None, device="cuda") -> SCFResult:
     """hf.py:237-353 (Pulay cDIIS)."""
     return _run(mol, "diis", tol, maxiter, precision, cutoff, fp32_cutoff, fb, device)
