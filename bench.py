@@ -147,7 +147,7 @@ def run_ours(args):
     nwater, basis = args.nwater, args.basis
     mol = workload(nwater, basis)
     fb = FockBuilder(mol, device=dev, cutoff=CUTOFF, fp32_cutoff=FP32_CUTOFF, precision="mixed")
-    r = scf_diis(mol, tol=1e-9, fb=fb, device=dev)
+    r = scf_diis(mol, tol=1e-9, fb=fb, device=dev, precision="fp64")
     D = r.D.contiguous()
     H = r.H
     stream = torch.cuda.current_stream()
@@ -165,7 +165,7 @@ def run_ours(args):
     # stats + per-launch profile of one build per precision
     prof = {}
     for prec in ("fp64", "mixed"):
-        fb.set_profiling(True)
+        fb.set_profiling(2)       # launches serialised on one stream: isolated per-kernel times
         fb.jk(D, precision=prec, out=(J, K), stats=True)
         prof[prec] = (dict(fb.last_stats), fb.slice_info())
         fb.set_profiling(False)

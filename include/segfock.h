@@ -141,8 +141,11 @@ int sf_eri_batch(sf_handle *h, const int32_t *quartets, int64_t nq, int32_t prec
 int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges,
                     int32_t natom, double *S, double *T, double *V, void *stream);
 
-/* Per-launch profiling of sf_fock_jk.  When on, every class kernel of a Fock
- * build is bracketed by CUDA events on the caller's stream; sf_slice_info
+/* Per-launch profiling of sf_fock_jk.  on = 1: every class kernel of a Fock
+ * build is bracketed by CUDA events on the stream it runs on (class launches
+ * run concurrently on streams forked from the caller's, so these times
+ * overlap); on = 2: the launches are also serialised on the caller's stream,
+ * so each time is that kernel alone; 0: off.  sf_slice_info
  * then reports, per launch ("slice" = one class in one precision), the work
  * and the device time of the last profiled build (waits for its events).
  * No counterpart in the reference (it only times whole SCF runs,

@@ -132,8 +132,9 @@ struct sf_handle {
   DBuf<double> d_cx, d_cy, d_cz, d_exps, d_coefs;
   DBuf<int> d_pa, d_pb, d_ppoff, d_pnp;
   DBuf<double> d_pq;
-  DBuf<double> d_pp64[6];
-  DBuf<float> d_pp32[6];
+  DBuf<double> d_pp64;
+  DBuf<float> d_pp32;
+  DBuf<float> d_cx32, d_cy32, d_cz32;
   DBuf<double> d_tab64;
   DBuf<float> d_tab32;
   DBuf<double> d_Jh, d_Kh;
@@ -147,7 +148,7 @@ struct sf_handle {
     int64_t quartets, prims;
     double flops;
   };
-  bool profiling = false;
+  int profiling = 0;              // 1: per-slice events; 2: also serialise launches
   std::vector<cudaEvent_t> ev;   // 2 per slice while profiling
   // side streams: the class launches of one build are independent (they only
   // add into Jh/Kh with atomics), so they are spread over kSideStreams
@@ -170,12 +171,11 @@ namespace {
 
 void fill_kparams(sf_handle *h) {
   KParams &k = h->kp;
-  k.sh = DevShells{h->d_l.p, h->d_nprim.p, h->d_ao.p, h->d_atom.p, h->d_cx.p, h->d_cy.p, h->d_cz.p};
+  k.sh = DevShells{h->d_l.p,  h->d_nprim.p, h->d_ao.p,   h->d_atom.p, h->d_cx.p,
+                   h->d_cy.p, h->d_cz.p,    h->d_cx32.p, h->d_cy32.p, h->d_cz32.p};
   k.pr = DevPairs{h->d_pa.p, h->d_pb.p, h->d_ppoff.p, h->d_pnp.p, h->d_pq.p};
-  k.p64 = DevPrims<double>{h->d_pp64[0].p, h->d_pp64[1].p, h->d_pp64[2].p, h->d_pp64[3].p, h->d_pp64[4].p,
-                           h->d_pp64[5].p};
-  k.p32 = DevPrims<float>{h->d_pp32[0].p, h->d_pp32[1].p, h->d_pp32[2].p, h->d_pp32[3].p, h->d_pp32[4].p,
-                          h->d_pp32[5].p};
+  k.p64 = DevPrims<double>{h->d_pp64.p};
+  k.p32 = DevPrims<float>{h->d_pp32.p};
   k.tab64 = h->d_tab64.p;
   k.tab32 = h->d_tab32.p;
   k.asym = host_tables().asym;
@@ -384,7 +384,18 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
 // (forked from st, joined back into st).  Events of the profiling mode
 // bracket each launch on its own stream.
 int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, double *Kh, cudaStream_t st,
-                  bool profiling, int *launches) {
+                  int profiling, int *launches) {
+  if (profiling == 2) {   // serialised on the caller's stream
+    for (size_t k = 0; k < h->slices.size(); ++k) {
+      const auto &s = h->slices[k];
+      SF_CK(cudaEventRecord(h->ev[2 * k], st));
+      if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, Jh, Kh, st));
+      else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, D32, Jh, Kh, st));
+      SF_CK(cudaEventRecord(h->ev[2 * k + 1], st));
+      if (launches) ++*launches;
+    }
+    return SF_OK;
+  }
   SF_CK(cudaEventRecord(h->fork_ev, st));
   bool used[sf_handle::kSideStreams] = {false};
   for (size_t k = 0; k < h->slices.size(); ++k) used[h->slice_stream[k]] = true;
@@ -503,10 +514,20 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
     }
   }
   h->cstart[kNumPairClass] = (int)h->pa.size();
-  for (int f = 0; f < 6; ++f) {
-    SF_CK(h->d_pp64[f].upload(pp[f]));
-    std::vector<float> v32(pp[f].begin(), pp[f].end());
-    SF_CK(h->d_pp32[f].upload(v32));
+  {
+    const size_t npp = pp[0].size();
+    std::vector<double> rec(npp * kPrimRec, 0.0);
+    for (size_t i = 0; i < npp; ++i)
+      for (int f = 0; f < 6; ++f) rec[i * kPrimRec + f] = pp[f][i];
+    SF_CK(h->d_pp64.upload(rec));
+    std::vector<float> rec32(rec.begin(), rec.end());
+    SF_CK(h->d_pp32.upload(rec32));
+    std::vector<float> c32(h->cx.begin(), h->cx.end());
+    SF_CK(h->d_cx32.upload(c32));
+    c32.assign(h->cy.begin(), h->cy.end());
+    SF_CK(h->d_cy32.upload(c32));
+    c32.assign(h->cz.begin(), h->cz.end());
+    SF_CK(h->d_cz32.upload(c32));
   }
   SF_CK(h->d_l.upload(h->l));
   SF_CK(h->d_nprim.upload(h->nprim));
@@ -559,7 +580,7 @@ void sf_destroy(sf_handle *h) {
 
 int sf_set_profiling(sf_handle *h, int32_t on) {
   if (!h) return fail(SF_EINVAL, "sf_set_profiling: NULL handle");
-  h->profiling = on != 0;
+  h->profiling = on < 0 ? 0 : on > 2 ? 2 : on;
   return SF_OK;
 }
 
@@ -733,7 +754,7 @@ int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int3
     to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, D32, (int64_t)nn);
     SF_CK(cudaGetLastError());
   }
-  int rc = launch_slices(h, D, D32, Jh, Kh, st, false, nullptr);
+  int rc = launch_slices(h, D, D32, Jh, Kh, st, 0, nullptr);
   if (rc) return rc;
   symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(Jh, Kh, J, K, n);
   SF_CK(cudaGetLastError());

@@ -73,7 +73,17 @@ __device__ __forceinline__ const double *tab_of<double>(const KParams &kp) { ret
 template <>
 __device__ __forceinline__ const float *tab_of<float>(const KParams &kp) { return kp.tab32; }
 
-// all n roots (u = t^2) and weights at x
+// vector type of two values
+template <typename R>
+struct Vec2;
+template <>
+struct Vec2<double> { using T = double2; };
+template <>
+struct Vec2<float> { using T = float2; };
+
+// all n roots (u = t^2) and weights at x.  Coefficient row k of an interval
+// holds the 2N values (u_0..u_{N-1}, w_0..w_{N-1}); rows are loaded as N
+// two-value vectors (the table offsets are all even).
 template <int N, typename R>
 __device__ __forceinline__ void rys_roots_all(const KParams &kp, R x, R (&u)[N], R (&w)[N]) {
   if (x >= (R)kTabXmax) {
@@ -85,22 +95,31 @@ __device__ __forceinline__ void rys_roots_all(const KParams &kp, R x, R (&u)[N],
     }
     return;
   }
+  using V = typename Vec2<R>::T;
   constexpr int D = TabDeg<R>::v;
   const int j = (int)x;
   const R s = (R)2 * (x - (R)j) - (R)1;
-  const R *c = tab_of<R>(kp) + rys_tab_offset(N, D) + j * (D + 1) * 2 * N;
+  const V *c = reinterpret_cast<const V *>(tab_of<R>(kp) + rys_tab_offset(N, D) + j * (D + 1) * 2 * N);
+  R f[2 * N];
 #pragma unroll
-  for (int f = 0; f < N; ++f) {
-    u[f] = __ldg(c + D * 2 * N + f);
-    w[f] = __ldg(c + D * 2 * N + N + f);
+  for (int i = 0; i < N; ++i) {
+    const V v = __ldg(c + D * N + i);
+    f[2 * i] = v.x;
+    f[2 * i + 1] = v.y;
   }
 #pragma unroll
   for (int k = D - 1; k >= 0; --k) {
 #pragma unroll
-    for (int f = 0; f < N; ++f) {
-      u[f] = u[f] * s + __ldg(c + k * 2 * N + f);
-      w[f] = w[f] * s + __ldg(c + k * 2 * N + N + f);
+    for (int i = 0; i < N; ++i) {
+      const V v = __ldg(c + k * N + i);
+      f[2 * i] = f[2 * i] * s + v.x;
+      f[2 * i + 1] = f[2 * i + 1] * s + v.y;
     }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    u[i] = f[i];
+    w[i] = f[N + i];
   }
 }
 
@@ -149,8 +168,7 @@ struct QC {
 // Vertical recurrence + horizontal transfer for one root and one direction.
 // Output I[((ia*(LB+1)+ib)*(LC+1)+ic)*(LD+1)+id].
 template <int LA, int LB, int LC, int LD, typename R>
-__device__ __forceinline__ void rys_2d(R g0, R c00, R c00p, R b00, R b10, R b01, R ab, R cd,
-                                       R (&I)[QC<LA, LB, LC, LD>::SZ]) {
+__device__ __forceinline__ void rys_2d(R g0, R c00, R c00p, R b00, R b10, R b01, R ab, R cd, R *__restrict__ I) {
   constexpr int LAB = LA + LB, LCD = LC + LD;
   R G[LAB + 1][LCD + 1];
   G[0][0] = g0;
@@ -217,6 +235,19 @@ struct QGeom {
 };
 
 template <typename R>
+__device__ __forceinline__ const R *centre_of(const DevShells &sh, int d);
+template <>
+__device__ __forceinline__ const double *centre_of<double>(const DevShells &sh, int d) {
+  return d == 0 ? sh.cx : d == 1 ? sh.cy : sh.cz;
+}
+template <>
+__device__ __forceinline__ const float *centre_of<float>(const DevShells &sh, int d) {
+  return d == 0 ? sh.cx32 : d == 1 ? sh.cy32 : sh.cz32;
+}
+
+// geometry in the working precision R (the FP32 kernels read single-precision
+// centres and never touch the FP64 pipe here)
+template <typename R>
 __device__ __forceinline__ QGeom<R> make_geom(const KParams &kp, int pab, int pcd, bool swap_ab, bool swap_cd) {
   QGeom<R> g;
   int a = kp.pr.a[pab], b = kp.pr.b[pab], c = kp.pr.a[pcd], d = kp.pr.b[pcd];
@@ -225,14 +256,11 @@ __device__ __forceinline__ QGeom<R> make_geom(const KParams &kp, int pab, int pc
   g.a = a; g.b = b; g.c = c; g.d = d;
   g.ab_off = kp.pr.poff[pab]; g.ab_n = kp.pr.np[pab];
   g.cd_off = kp.pr.poff[pcd]; g.cd_n = kp.pr.np[pcd];
-  const double ax = kp.sh.cx[a], ay = kp.sh.cy[a], az = kp.sh.cz[a];
-  const double bx = kp.sh.cx[b], by = kp.sh.cy[b], bz = kp.sh.cz[b];
-  const double cx = kp.sh.cx[c], cy = kp.sh.cy[c], cz = kp.sh.cz[c];
-  const double dx = kp.sh.cx[d], dy = kp.sh.cy[d], dz = kp.sh.cz[d];
-  g.Ax = (R)ax; g.Ay = (R)ay; g.Az = (R)az;
-  g.Cx = (R)cx; g.Cy = (R)cy; g.Cz = (R)cz;
-  g.ABx = (R)(ax - bx); g.ABy = (R)(ay - by); g.ABz = (R)(az - bz);
-  g.CDx = (R)(cx - dx); g.CDy = (R)(cy - dy); g.CDz = (R)(cz - dz);
+  const R *X = centre_of<R>(kp.sh, 0), *Y = centre_of<R>(kp.sh, 1), *Z = centre_of<R>(kp.sh, 2);
+  g.Ax = X[a]; g.Ay = Y[a]; g.Az = Z[a];
+  g.Cx = X[c]; g.Cy = Y[c]; g.Cz = Z[c];
+  g.ABx = g.Ax - X[b]; g.ABy = g.Ay - Y[b]; g.ABz = g.Az - Z[b];
+  g.CDx = g.Cx - X[d]; g.CDy = g.Cy - Y[d]; g.CDz = g.Cz - Z[d];
   return g;
 }
 
@@ -243,24 +271,37 @@ struct PQ {
   R r2, aq, ap, i2p, i2q, x, pref;
 };
 
+// one primitive-pair record as (p, Px, Py, Pz) and (K~, 0.5/p)
+template <typename R>
+__device__ __forceinline__ void load_rec(const R *rec, R &p, R &px, R &py, R &pz, R &k, R &i2p);
+template <>
+__device__ __forceinline__ void load_rec<float>(const float *rec, float &p, float &px, float &py, float &pz, float &k,
+                                                float &i2p) {
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(rec));
+  const float2 b = __ldg(reinterpret_cast<const float2 *>(rec + 4));
+  p = a.x; px = a.y; py = a.z; pz = a.w; k = b.x; i2p = b.y;
+}
+template <>
+__device__ __forceinline__ void load_rec<double>(const double *rec, double &p, double &px, double &py, double &pz,
+                                                 double &k, double &i2p) {
+  const double2 a = __ldg(reinterpret_cast<const double2 *>(rec));
+  const double2 b = __ldg(reinterpret_cast<const double2 *>(rec + 2));
+  const double2 c = __ldg(reinterpret_cast<const double2 *>(rec + 4));
+  p = a.x; px = a.y; py = b.x; pz = b.y; k = c.x; i2p = c.y;
+}
+
 template <typename R>
 __device__ __forceinline__ void load_prim_ab(const KParams &kp, const QGeom<R> &g, int ip, PQ<R> &s, R &p, R &px,
                                              R &py, R &pz, R &kab) {
-  const DevPrims<R> &P = prims_of<R>(kp);
-  const int i = g.ab_off + ip;
-  p = __ldg(P.p + i); px = __ldg(P.px + i); py = __ldg(P.py + i); pz = __ldg(P.pz + i);
-  kab = __ldg(P.k + i); s.i2p = __ldg(P.inv2p + i);
+  load_rec<R>(prims_of<R>(kp).rec + (size_t)(g.ab_off + ip) * kPrimRec, p, px, py, pz, kab, s.i2p);
   s.pax = px - g.Ax; s.pay = py - g.Ay; s.paz = pz - g.Az;
 }
 
 template <typename R>
 __device__ __forceinline__ void load_prim_cd(const KParams &kp, const QGeom<R> &g, int iq, PQ<R> &s, R p, R px, R py,
                                              R pz, R kab) {
-  const DevPrims<R> &P = prims_of<R>(kp);
-  const int i = g.cd_off + iq;
-  const R q = __ldg(P.p + i), qx = __ldg(P.px + i), qy = __ldg(P.py + i), qz = __ldg(P.pz + i);
-  const R kcd = __ldg(P.k + i);
-  s.i2q = __ldg(P.inv2p + i);
+  R q, qx, qy, qz, kcd;
+  load_rec<R>(prims_of<R>(kp).rec + (size_t)(g.cd_off + iq) * kPrimRec, q, qx, qy, qz, kcd, s.i2q);
   s.qcx = qx - g.Cx; s.qcy = qy - g.Cy; s.qcz = qz - g.Cz;
   s.pqx = px - qx; s.pqy = py - qy; s.pqz = pz - qz;
   const R rr = rsqrt_nr(p + q);
@@ -271,6 +312,19 @@ __device__ __forceinline__ void load_prim_cd(const KParams &kp, const QGeom<R> &
   s.x = rho * (s.pqx * s.pqx + s.pqy * s.pqy + s.pqz * s.pqz);
   s.pref = kab * kcd * rr;
 }
+
+// float -> double without the FP64 pipe: re-pack sign, exponent (rebias
+// 127 -> 1023) and mantissa with 32-bit integer operations.  Zeros and
+// single-precision subnormals (< 1.2e-38) become +-0; inf/nan stay inf/nan.
+__device__ __forceinline__ double f2d_alu(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu, sgn = u & 0x80000000u;
+  if (e == 0u) return __hiloint2double((int)sgn, 0);
+  const unsigned de = e == 0xffu ? 0x7ffu : e + 896u;
+  return __hiloint2double((int)(sgn | (de << 20) | (m >> 3)), (int)(m << 29));
+}
+__device__ __forceinline__ double to_f64(float f) { return f2d_alu(f); }
+__device__ __forceinline__ double to_f64(double f) { return f; }
 
 // ---------------------------------------------------------------------------
 // T == 1: whole quartet in registers; acc[o] unnormalised
@@ -321,8 +375,12 @@ template <int LA, int LB, int LC, int LD, typename R, int T>
 struct Grp {
   using Q = QC<LA, LB, LC, LD>;
   static constexpr int NPER = (Q::NABCD + T - 1) / T;
-  static constexpr int TABN = 3 * Q::NR * Q::SZ;
-  static constexpr int BUFN = TABN > Q::NABCD ? TABN : Q::NABCD;
+  static constexpr int TABN = 3 * Q::NR * Q::SZ;            // 2-D tables of one primitive quartet
+  static constexpr int ROOTS = TABN;                         // then u_r, w_r
+  static constexpr int NEED = (TABN + 2 * Q::NR) > Q::NABCD ? (TABN + 2 * Q::NR) : Q::NABCD;
+  // odd stride (in elements) between the buffers of neighbouring groups so
+  // that equal offsets of different groups fall into different banks
+  static constexpr int BUFN = NEED | 1;
 };
 
 template <int LA, int LB, int LC, int LD, typename R, int T>
@@ -351,10 +409,17 @@ __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R
       cur = ip;
     }
     load_prim_cd<R>(kp, g, iq, s, pp, px, py, pz, kab);
-    for (int task = t; task < 3 * NR; task += T) {
-      const int r = task % NR, d = task / NR;
+    // each root once: lane t evaluates roots t, t+T, ... into the group buffer
+    for (int r = t; r < NR; r += T) {
       R uu, ww;
       rys_root_one<NR, R>(kp, s.x, r, uu, ww);
+      tab[GP::ROOTS + r] = uu;
+      tab[GP::ROOTS + NR + r] = ww;
+    }
+    __syncwarp(gmask);
+    for (int task = t; task < 3 * NR; task += T) {
+      const int r = task % NR, d = task / NR;
+      const R uu = tab[GP::ROOTS + r], ww = tab[GP::ROOTS + NR + r];
       const R b00 = (R)0.5 * s.r2 * uu;
       const R b10 = s.i2p * ((R)1 - s.aq * uu);
       const R b01 = s.i2q * ((R)1 - s.ap * uu);
@@ -365,11 +430,7 @@ __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R
       const R ab = d == 0 ? g.ABx : d == 1 ? g.ABy : g.ABz;
       const R cd = d == 0 ? g.CDx : d == 1 ? g.CDy : g.CDz;
       const R g0 = d == 2 ? s.pref * ww : (R)1;
-      R I[SZ];
-      rys_2d<LA, LB, LC, LD, R>(g0, pa - tq * pq, qc + tp * pq, b00, b10, b01, ab, cd, I);
-      R *dst = tab + (d * NR + r) * SZ;
-#pragma unroll
-      for (int i = 0; i < SZ; ++i) dst[i] = I[i];
+      rys_2d<LA, LB, LC, LD, R>(g0, pa - tq * pq, qc + tp * pq, b00, b10, b01, ab, cd, tab + (d * NR + r) * SZ);
     }
     __syncwarp(gmask);
 #pragma unroll
@@ -404,7 +465,7 @@ __device__ __forceinline__ void reduce_psplit(R (&acc)[N], int P, unsigned qmask
 // ---------------------------------------------------------------------------
 template <int LA, int LB, int LC, int LD, typename R>
 __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, const R (&acc)[QC<LA, LB, LC, LD>::NABCD],
-                                          double scale, const R *__restrict__ D, double *Jh, double *Kh) {
+                                          R scale, const R *__restrict__ D, double *Jh, double *Kh) {
   using Q = QC<LA, LB, LC, LD>;
   const int n = kp.nao;
   const int a0 = kp.sh.ao[g.a], b0 = kp.sh.ao[g.b], c0 = kp.sh.ao[g.c], d0 = kp.sh.ao[g.d];
@@ -422,7 +483,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id)
           s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (c0 + ic) * n + d0 + id);
-      atomicAdd(Jh + (a0 + ia) * n + b0 + ib, 2.0 * scale * (double)s);
+      atomicAdd(Jh + (a0 + ia) * n + b0 + ib, to_f64((R)2 * scale * s));
     }
 #pragma unroll
   for (int ic = 0; ic < Q::NC; ++ic)
@@ -434,7 +495,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 #pragma unroll
         for (int ib = 0; ib < Q::NB; ++ib)
           s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + b0 + ib);
-      atomicAdd(Jh + (c0 + ic) * n + d0 + id, 2.0 * scale * (double)s);
+      atomicAdd(Jh + (c0 + ic) * n + d0 + id, to_f64((R)2 * scale * s));
     }
 #pragma unroll
   for (int ia = 0; ia < Q::NA; ++ia)
@@ -446,7 +507,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id)
           s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (b0 + ib) * n + d0 + id);
-      atomicAdd(Kh + (a0 + ia) * n + c0 + ic, scale * (double)s);
+      atomicAdd(Kh + (a0 + ia) * n + c0 + ic, to_f64(scale * s));
     }
 #pragma unroll
   for (int ib = 0; ib < Q::NB; ++ib)
@@ -458,7 +519,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id)
           s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + d0 + id);
-      atomicAdd(Kh + (b0 + ib) * n + c0 + ic, scale * (double)s);
+      atomicAdd(Kh + (b0 + ib) * n + c0 + ic, to_f64(scale * s));
     }
 #pragma unroll
   for (int ia = 0; ia < Q::NA; ++ia)
@@ -470,7 +531,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic)
           s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (b0 + ib) * n + c0 + ic);
-      atomicAdd(Kh + (a0 + ia) * n + d0 + id, scale * (double)s);
+      atomicAdd(Kh + (a0 + ia) * n + d0 + id, to_f64(scale * s));
     }
 #pragma unroll
   for (int ib = 0; ib < Q::NB; ++ib)
@@ -482,7 +543,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic)
           s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + c0 + ic);
-      atomicAdd(Kh + (b0 + ib) * n + d0 + id, scale * (double)s);
+      atomicAdd(Kh + (b0 + ib) * n + d0 + id, to_f64(scale * s));
     }
 }
 
@@ -491,7 +552,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
                                            const R (&acc)[Grp<LA, LB, LC, LD, R, T>::NPER], R *buf, int t,
-                                           unsigned gmask, double scale, const R *__restrict__ D, double *Jh,
+                                           unsigned gmask, R scale, const R *__restrict__ D, double *Jh,
                                            double *Kh) {
   using Q = QC<LA, LB, LC, LD>;
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
@@ -513,32 +574,32 @@ __device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
       const int ia = e / NB, ib = e % NB;
       for (int ic = 0; ic < NC; ++ic)
         for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (c0 + ic) * n + d0 + id);
-      atomicAdd(Jh + (a0 + ia) * n + b0 + ib, 2.0 * scale * (double)s);
+      atomicAdd(Jh + (a0 + ia) * n + b0 + ib, to_f64((R)2 * scale * s));
     } else if (e < E1) {
       const int ic = (e - E0) / ND, id = (e - E0) % ND;
       for (int ia = 0; ia < NA; ++ia)
         for (int ib = 0; ib < NB; ++ib) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + b0 + ib);
-      atomicAdd(Jh + (c0 + ic) * n + d0 + id, 2.0 * scale * (double)s);
+      atomicAdd(Jh + (c0 + ic) * n + d0 + id, to_f64((R)2 * scale * s));
     } else if (e < E2) {
       const int ia = (e - E1) / NC, ic = (e - E1) % NC;
       for (int ib = 0; ib < NB; ++ib)
         for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (b0 + ib) * n + d0 + id);
-      atomicAdd(Kh + (a0 + ia) * n + c0 + ic, scale * (double)s);
+      atomicAdd(Kh + (a0 + ia) * n + c0 + ic, to_f64(scale * s));
     } else if (e < E3) {
       const int ib = (e - E2) / NC, ic = (e - E2) % NC;
       for (int ia = 0; ia < NA; ++ia)
         for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + d0 + id);
-      atomicAdd(Kh + (b0 + ib) * n + c0 + ic, scale * (double)s);
+      atomicAdd(Kh + (b0 + ib) * n + c0 + ic, to_f64(scale * s));
     } else if (e < E4) {
       const int ia = (e - E3) / ND, id = (e - E3) % ND;
       for (int ib = 0; ib < NB; ++ib)
         for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * __ldg(D + (b0 + ib) * n + c0 + ic);
-      atomicAdd(Kh + (a0 + ia) * n + d0 + id, scale * (double)s);
+      atomicAdd(Kh + (a0 + ia) * n + d0 + id, to_f64(scale * s));
     } else {
       const int ib = (e - E4) / ND, id = (e - E4) % ND;
       for (int ia = 0; ia < NA; ++ia)
         for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + c0 + ic);
-      atomicAdd(Kh + (b0 + ib) * n + d0 + id, scale * (double)s);
+      atomicAdd(Kh + (b0 + ib) * n + d0 + id, to_f64(scale * s));
     }
   }
 #undef V4
@@ -571,10 +632,10 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
   const int i = ij.x, j = ij.y;
   const int pab = w.x0 + i, pcd = w.y0 + j;
   const QGeom<R> g = make_geom<R>(kp, pab, pcd, false, false);
-  double scale = 1.0;
-  if (g.a == g.b) scale *= 0.5;
-  if (g.c == g.d) scale *= 0.5;
-  if (w.same && i == j) scale *= 0.5;
+  R scale = (R)1;
+  if (g.a == g.b) scale *= (R)0.5;
+  if (g.c == g.d) scale *= (R)0.5;
+  if (w.same && i == j) scale *= (R)0.5;
   const int lane = threadIdx.x & 31;
   const unsigned qmask = (TP == 32) ? 0xffffffffu : (((1u << TP) - 1u) << (lane & ~(TP - 1)));
   if constexpr (T == 1) {
@@ -622,7 +683,7 @@ __global__ void __launch_bounds__(kBlock) eri_kernel(KParams kp, EriWork w) {
     eval_t1<LA, LB, LC, LD, R>(kp, g, acc);
 #pragma unroll
     for (int o = 0; o < Q::NABCD; ++o)
-      out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = (double)(acc[o] * (R)Q::norm(o));
+      out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = to_f64(acc[o] * (R)Q::norm(o));
   } else {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using GP = Grp<LA, LB, LC, LD, R, T>;
@@ -634,7 +695,7 @@ __global__ void __launch_bounds__(kBlock) eri_kernel(KParams kp, EriWork w) {
     for (int k = 0; k < GP::NPER; ++k) {
       const int o = t + k * T;
       if (o < Q::NABCD)
-        out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = (double)(acc[k] * (R)Q::norm(o));
+        out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = to_f64(acc[k] * (R)Q::norm(o));
     }
   }
 }

@@ -7,7 +7,7 @@
 //              sf_schwarz, sorted by Schwarz bound Q_ab descending inside each
 //              class.  A pair record holds a, b, the offset and count of its
 //              primitive pairs, and Q_ab.
-//   prims    : SoA over all primitive pairs (alpha_i, beta_j) of all pairs:
+//   prims    : one 8-value record per primitive pair (alpha_i, beta_j):
 //              p = alpha+beta, P = (alpha A + beta B)/p, 0.5/p and
 //              K~ = c_i c_j exp(-alpha beta/p |AB|^2) sqrt(2) pi^(5/4) / p,
 //              in FP64 and FP32.  K~_ab K~_cd / sqrt(p+q) is the full
@@ -62,6 +62,7 @@ __host__ __device__ constexpr double cart_norm(int l, int i) {
 struct DevShells {
   const int *l, *nprim, *ao, *atom;
   const double *cx, *cy, *cz;
+  const float *cx32, *cy32, *cz32;   // single-precision copies for the FP32 kernels
 };
 
 struct DevPairs {
@@ -69,9 +70,13 @@ struct DevPairs {
   const double *q;
 };
 
+// primitive-pair records (array of structures, 8 values each so that a
+// record is read with two vector loads in FP32 and three in FP64):
+//   [p, Px, Py, Pz, K~, 0.5/p, 0, 0]
+constexpr int kPrimRec = 8;
 template <typename R>
 struct DevPrims {
-  const R *p, *px, *py, *pz, *k, *inv2p;
+  const R *rec;
 };
 
 struct RysAsym {

@@ -137,8 +137,10 @@ class FockBuilder:
             self.last_stats = st.as_dict()
         return J, K
 
-    def set_profiling(self, on: bool = True):
-        _lib.check(_lib.lib().sf_set_profiling(self._h, 1 if on else 0))
+    def set_profiling(self, on=True):
+        """True/1: time every class launch; 2: also serialise the launches on
+        the caller's stream so each time is the kernel alone."""
+        _lib.check(_lib.lib().sf_set_profiling(self._h, int(on)))
 
     def slice_info(self):
         """Per-launch work and (when profiling) device time of the last Fock build."""
