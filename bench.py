@@ -196,6 +196,15 @@ def run_ours(args):
     clocks = clock_sampler_stop(proc, fh, clk_path) if rank == 0 else None
     if world > 1:
         dist.barrier()
+    # forces: one complete nuclear gradient (backward from the converged SCF)
+    from segfault_py_gb300.grad import rhf_gradient
+    t_f = {}
+    for prec in ("mixed", "fp64"):
+        t_f[prec] = time_steps(lambda: rhf_gradient(mol, r, fb, precision=prec), max(3, args.steps // 4),
+                               args.warmup, flush, stream)
+    g64 = rhf_gradient(mol, r, fb, precision="fp64")
+    gmx = rhf_gradient(mol, r, fb, precision="mixed")
+    grad_err = float((gmx - g64).abs().max())
     ms_mx, ms_64, ms_e2e = float(np.sum(t_mx)), float(np.sum(t_64)), float(np.sum(t_e2e))
     if world > 1:
         tt = torch.tensor([ms_mx, ms_64, ms_e2e], dtype=torch.float64, device=dev)
@@ -236,6 +245,9 @@ def run_ours(args):
         "quartets": {"fp64": st_mx["quartets_fp64"], "fp32": st_mx["quartets_fp32"],
                      "unscreened": st_mx["quartets_total"]},
         "energy_error_mixed_vs_fp64": emx - e64,
+        "forces": {"value": world * 1e3 / float(np.mean(t_f["mixed"])), "unit": "forces/s",
+                   "fp64": world * 1e3 / float(np.mean(t_f["fp64"])),
+                   "max_grad_error_mixed_vs_fp64": grad_err, "unit_error": "Eh/bohr"},
         "gpu_launches": int(st_mx["launches"]) * steps * 2 + int(st_64["launches"]) * steps,
         "roofline": {"bound": dom_prec, "achieved": achieved, "peak": peaks[dom_prec], "unit": "TFLOP/s",
                      "frac": achieved / peaks[dom_prec] if peaks[dom_prec] else None, "traffic": None,

@@ -141,6 +141,23 @@ int sf_eri_batch(sf_handle *h, const int32_t *quartets, int64_t nq, int32_t prec
 int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges,
                     int32_t natom, double *S, double *T, double *V, void *stream);
 
+/* Two-electron part of the analytic RHF nuclear gradient (no counterpart in
+ * the reference, which has no gradients):
+ *   grad[3*A + d] += sum_{pqrs} G_pqrs d(pq|rs)/dR_{A,d},
+ *   G_pqrs = 1/2 D_pq D_rs - 1/8 (D_pr D_qs + D_ps D_qr),
+ * i.e. the derivative of 1/2 sum_pq D_pq (J - K/2)_pq at fixed D, over the
+ * same screened quartets and precision split as sf_fock_jk.  grad (device,
+ * 3 doubles per atom index used by the shells) is accumulated, not zeroed. */
+int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, double cutoff,
+               double fp32_cutoff, void *stream);
+
+/* One-electron part of the gradient: derivatives of sum_pq D_pq (T+V)_pq
+ * - W_pq S_pq with respect to the basis centres and, for V, the nuclei
+ * (W = energy-weighted density 2 sum_occ e_i C_pi C_qi).  atom_xyz/charges as
+ * in sf_one_electron; grad accumulated. */
+int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *charges, int32_t natom,
+                         const double *D, const double *W, double *grad, void *stream);
+
 /* Per-launch profiling of sf_fock_jk.  on = 1: every class kernel of a Fock
  * build is bracketed by CUDA events on the stream it runs on (class launches
  * run concurrently on streams forked from the caller's, so these times

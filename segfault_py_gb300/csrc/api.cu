@@ -380,6 +380,24 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
   return SF_OK;
 }
 
+// Run fn(k, stream) for every slice k on its side stream (forked from st,
+// joined back into st).
+template <typename F>
+int fan_out(sf_handle *h, cudaStream_t st, F &&fn) {
+  SF_CK(cudaEventRecord(h->fork_ev, st));
+  bool used[sf_handle::kSideStreams] = {false};
+  for (size_t k = 0; k < h->slices.size(); ++k) used[h->slice_stream[k]] = true;
+  for (int j = 0; j < sf_handle::kSideStreams; ++j)
+    if (used[j]) SF_CK(cudaStreamWaitEvent(h->side[j], h->fork_ev, 0));
+  for (size_t k = 0; k < h->slices.size(); ++k) SF_CK(fn(k, h->side[h->slice_stream[k]]));
+  for (int j = 0; j < sf_handle::kSideStreams; ++j)
+    if (used[j]) {
+      SF_CK(cudaEventRecord(h->join_ev[j], h->side[j]));
+      SF_CK(cudaStreamWaitEvent(st, h->join_ev[j], 0));
+    }
+  return SF_OK;
+}
+
 // Launch every slice of the current quartet lists on the side streams
 // (forked from st, joined back into st).  Events of the profiling mode
 // bracket each launch on its own stream.
@@ -485,7 +503,7 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   h->nao = nao;
   // canonical shell pairs, grouped by pair class
   const double kpre = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
-  std::vector<double> pp[6];
+  std::vector<double> pp[8];
   for (int pc = 0; pc < kNumPairClass; ++pc) {
     h->cstart[pc] = (int)h->pa.size();
     const int la = kPairL[pc][0], lb = kPairL[pc][1];
@@ -509,6 +527,8 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
             pp[3].push_back((al * h->cz[a] + be * h->cz[b]) / p);
             pp[4].push_back(h->coefs[i] * h->coefs[j] * std::exp(-al * be / p * AB2) * kpre / p);
             pp[5].push_back(0.5 / p);
+            pp[6].push_back(al);   // exponents of the two primitives (gradients)
+            pp[7].push_back(be);
           }
       }
     }
@@ -518,7 +538,7 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
     const size_t npp = pp[0].size();
     std::vector<double> rec(npp * kPrimRec, 0.0);
     for (size_t i = 0; i < npp; ++i)
-      for (int f = 0; f < 6; ++f) rec[i * kPrimRec + f] = pp[f][i];
+      for (int f = 0; f < kPrimRec; ++f) rec[i * kPrimRec + f] = pp[f][i];
     SF_CK(h->d_pp64.upload(rec));
     std::vector<float> rec32(rec.begin(), rec.end());
     SF_CK(h->d_pp32.upload(rec32));
@@ -557,6 +577,8 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   SF_CK(prepare_jk_f64());
   SF_CK(prepare_jk_f32());
   SF_CK(prepare_eri());
+  SF_CK(prepare_grad_f64());
+  SF_CK(prepare_grad_f32());
   *out = guard.release();
   g_err.clear();
   return SF_OK;
@@ -758,6 +780,52 @@ int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int3
   if (rc) return rc;
   symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(Jh, Kh, J, K, n);
   SF_CK(cudaGetLastError());
+  return SF_OK;
+}
+
+int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, double cutoff, double fp32_cutoff,
+               void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_grad_jk: NULL handle");
+  if (!D || !grad) return fail(SF_EINVAL, "sf_grad_jk: NULL pointer");
+  if (precision < SF_PREC_FP64 || precision > SF_PREC_MIXED) return fail(SF_EINVAL, "sf_grad_jk: bad precision");
+  if (!(cutoff >= 0.0) || !(fp32_cutoff >= 0.0)) return fail(SF_EINVAL, "sf_grad_jk: bad cutoff");
+  if (!h->have_schwarz) return fail(SF_ESTATE, "sf_grad_jk: call sf_schwarz first");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = build_work(h, precision, cutoff, fp32_cutoff);
+  if (rc) return rc;
+  const size_t nn = (size_t)h->nao * h->nao;
+  bool need32 = false;
+  for (const auto &s : h->slices) need32 |= s.prec == 1;
+  if (need32) {
+    to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, h->d_D32.p, (int64_t)nn);
+    SF_CK(cudaGetLastError());
+  }
+  return fan_out(h, st, [&](size_t k, cudaStream_t ss) {
+    const auto &s = h->slices[k];
+    return s.prec == 0 ? launch_grad_f64(s.cls, h->kp, s.w, D, grad, ss)
+                       : launch_grad_f32(s.cls, h->kp, s.w, h->d_D32.p, grad, ss);
+  });
+}
+
+int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *charges, int32_t natom, const double *D,
+                         const double *W, double *grad, void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_grad_one_electron: NULL handle");
+  if (!D || !W || !grad || natom < 0 || (natom > 0 && (!atom_xyz || !charges)))
+    return fail(SF_EINVAL, "sf_grad_one_electron: bad arguments");
+  DeviceGuard g(h->device);
+  OneParams P;
+  P.sh = h->kp.sh;
+  P.exps = h->d_exps.p;
+  P.coefs = h->d_coefs.p;
+  P.poff = h->d_spoff.p;
+  P.nshell = h->nshell;
+  P.nao = h->nao;
+  P.atom_xyz = atom_xyz;
+  P.charges = charges;
+  P.natom = natom;
+  P.S = P.T = P.V = nullptr;
+  SF_CK(launch_one_electron_grad(P, D, W, grad, (cudaStream_t)stream));
   return SF_OK;
 }
 

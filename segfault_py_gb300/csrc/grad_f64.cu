@@ -1,0 +1,44 @@
+// grad_f64.cu -- FP64 two-electron gradient kernels, one per class.
+#include "classes.h"
+#include "grad.cuh"
+#include "launch.h"
+
+namespace sf {
+
+template <int LA, int LB, int LC, int LD>
+static cudaError_t run_grad64(const KParams &kp, const ClassWork &w, const double *D, double *grad, cudaStream_t st) {
+  constexpr int T = tgrad(QC<LA, LB, LC, LD>::NABCD);
+  if (w.n <= 0) return cudaSuccess;
+  int P = w.psplit < 1 ? 1 : w.psplit;
+  while (T * P > 32) P >>= 1;
+  ClassWork w2 = w;
+  w2.psplit = P;
+  const int G = kBlock / (T * P);
+  constexpr size_t smem = grad_smem<LA, LB, LC, LD, double>();
+  grad_kernel<LA, LB, LC, LD, double, T><<<(unsigned)((w.n + G - 1) / G), kBlock, smem, st>>>(kp, w2, D, grad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_f64(int cls, const KParams &kp, const ClassWork &w, const double *D, double *grad,
+                            cudaStream_t st) {
+  switch (cls) {
+#define SF_CASE(id, la, lb, lc, ld, t64, t32) \
+  case id: return run_grad64<la, lb, lc, ld>(kp, w, D, grad, st);
+    SF_CLASS_LIST(SF_CASE)
+#undef SF_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t prepare_grad_f64() {
+  cudaError_t e = cudaSuccess;
+#define SF_PREP(id, la, lb, lc, ld, t64, t32)                                                               \
+  if (e == cudaSuccess)                                                                                     \
+    e = prep_smem(grad_kernel<la, lb, lc, ld, double, tgrad(QC<la, lb, lc, ld>::NABCD)>,                    \
+                  grad_smem<la, lb, lc, ld, double>());
+  SF_CLASS_LIST(SF_PREP)
+#undef SF_PREP
+  return e;
+}
+
+}  // namespace sf

@@ -13,6 +13,12 @@ cudaError_t launch_eri(int cls, int fp32, const KParams &kp, const EriWork &w, c
 // Schwarz bounds of pair class pc (0..5) over pairs [p0, p0+n)
 cudaError_t launch_schwarz(int pc, const KParams &kp, int p0, int n, double *qout, cudaStream_t st);
 
+cudaError_t launch_grad_f64(int cls, const KParams &kp, const ClassWork &w, const double *D, double *grad,
+                            cudaStream_t st);
+cudaError_t launch_grad_f32(int cls, const KParams &kp, const ClassWork &w, const float *D, double *grad,
+                            cudaStream_t st);
+cudaError_t prepare_grad_f64();
+cudaError_t prepare_grad_f32();
 cudaError_t prepare_jk_f64();
 cudaError_t prepare_jk_f32();
 cudaError_t prepare_eri();
@@ -29,6 +35,10 @@ struct OneParams {
 };
 
 cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st);
+// gradient of sum_ij D_ij (T+V)_ij - W_ij S_ij (derivatives of the basis
+// centres and, for V, of the nuclei), accumulated into grad[3*natom]
+cudaError_t launch_one_electron_grad(const OneParams &P, const double *D, const double *W, double *grad,
+                                     cudaStream_t st);
 
 // smem bytes of a group kernel
 template <int LA, int LB, int LC, int LD, typename R, int T>

@@ -200,4 +200,158 @@ cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Gradient of E1 = sum_ij D_ij (T_ij + V_ij) - W_ij S_ij.  With D, W and the
+// operators symmetric, d/dR sum_ij D_ij O_ij = 2 sum_ij D_ij <d phi_i/dR|O|phi_j>,
+// so one thread per ordered shell pair (a, b) differentiates the bra function
+// only, d phi_a / dA = 2 alpha phi_{a+1} - a phi_{a-1}, and counts it twice.
+// V also depends on the nucleus C: by translational invariance of
+// <a|1/r_C|b>, dV/dC = -(dV/dA + dV/dB), which over all ordered pairs is
+// -2 sum_ij D_ij <d phi_i/dA|1/r_C|phi_j>.
+// ---------------------------------------------------------------------------
+template <int LA, int LB>
+__device__ void one_pair_grad(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b) {
+  constexpr int NA = ncart(LA), NB = ncart(LB);
+  constexpr int LE = LA + 1;                 // bra shifted up by one
+  constexpr int L = LA + LB + 1;
+  const double pi = 3.14159265358979323846;
+  const double A[3] = {P.sh.cx[a], P.sh.cy[a], P.sh.cz[a]};
+  const double B[3] = {P.sh.cx[b], P.sh.cy[b], P.sh.cz[b]};
+  const int a0 = P.sh.ao[a], b0 = P.sh.ao[b], n = P.nao;
+  double Dab[NA][NB], Wab[NA][NB];
+  for (int i = 0; i < NA; ++i)
+    for (int j = 0; j < NB; ++j) {
+      const double nrm = cart_norm(LA, i) * cart_norm(LB, j);
+      Dab[i][j] = Dm[(a0 + i) * n + b0 + j] * nrm;
+      Wab[i][j] = Wm[(a0 + i) * n + b0 + j] * nrm;
+    }
+  double gA[3] = {0.0, 0.0, 0.0};
+  double E[3][LE + 1][LB + 3][LE + LB + 3];
+  // overlap and kinetic: Pulay term -W dS and D dT
+  for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
+    for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
+      const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
+      const double cc = P.coefs[ia] * P.coefs[ib];
+      for (int d = 0; d < 3; ++d) {
+        const double Pd = (al * A[d] + be * B[d]) / p, X = A[d] - B[d];
+        hermite_e<LE, LB + 2>(p, Pd - A[d], Pd - B[d], exp(-mu * X * X), E[d]);
+      }
+      const double sp = pow(pi / p, 1.5);
+      for (int i = 0; i < NA; ++i)
+        for (int j = 0; j < NB; ++j) {
+          const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
+          for (int d = 0; d < 3; ++d) {
+            double dS = 0.0, dT = 0.0;
+            for (int sgn = 0; sgn < 2; ++sgn) {
+              int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
+              const int ad = ax[d];
+              if (sgn == 1 && ad == 0) continue;
+              ax[d] += sgn == 0 ? 1 : -1;
+              const double f = sgn == 0 ? 2.0 * al : -(double)ad;
+              const double sx = E[0][ax[0]][bx[0]][0], sy = E[1][ax[1]][bx[1]][0], sz = E[2][ax[2]][bx[2]][0];
+              const double s0 = sx * sy * sz * sp;
+              double t = be * (2 * (bx[0] + bx[1] + bx[2]) + 3) * s0;
+              t -= 2.0 * be * be * sp *
+                   (E[0][ax[0]][bx[0] + 2][0] * sy * sz + sx * E[1][ax[1]][bx[1] + 2][0] * sz +
+                    sx * sy * E[2][ax[2]][bx[2] + 2][0]);
+              if (bx[0] >= 2) t -= 0.5 * bx[0] * (bx[0] - 1) * sp * E[0][ax[0]][bx[0] - 2][0] * sy * sz;
+              if (bx[1] >= 2) t -= 0.5 * bx[1] * (bx[1] - 1) * sp * sx * E[1][ax[1]][bx[1] - 2][0] * sz;
+              if (bx[2] >= 2) t -= 0.5 * bx[2] * (bx[2] - 1) * sp * sx * sy * E[2][ax[2]][bx[2] - 2][0];
+              dS += f * s0;
+              dT += f * t;
+            }
+            gA[d] += cc * (Dab[i][j] * dT - Wab[i][j] * dS);
+          }
+        }
+    }
+  // nuclear attraction, nucleus by nucleus
+  for (int at = 0; at < P.natom; ++at) {
+    const double Cc[3] = {P.atom_xyz[3 * at], P.atom_xyz[3 * at + 1], P.atom_xyz[3 * at + 2]};
+    double gC[3] = {0.0, 0.0, 0.0};
+    for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
+      for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
+        const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
+        const double cc = P.coefs[ia] * P.coefs[ib];
+        double Pc[3];
+        for (int d = 0; d < 3; ++d) {
+          Pc[d] = (al * A[d] + be * B[d]) / p;
+          const double X = A[d] - B[d];
+          hermite_e<LE, LB + 2>(p, Pc[d] - A[d], Pc[d] - B[d], exp(-mu * X * X), E[d]);
+        }
+        const double pc[3] = {Pc[0] - Cc[0], Pc[1] - Cc[1], Pc[2] - Cc[2]};
+        double F[L + 1];
+        boys_array(L, p * (pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]), F);
+        double R[L + 1][L + 1][L + 1][L + 1];
+        for (int m = 0; m <= L; ++m) {
+          double f = F[m];
+          for (int k = 0; k < m; ++k) f *= -2.0 * p;
+          R[m][0][0][0] = f;
+        }
+        for (int m = L - 1; m >= 0; --m)
+          for (int t = 0; t <= L - m; ++t)
+            for (int u = 0; u <= L - m - t; ++u)
+              for (int w = 0; w <= L - m - t - u; ++w) {
+                if (t + u + w == 0) continue;
+                double r;
+                if (t > 0) r = (t > 1 ? (t - 1) * R[m + 1][t - 2][u][w] : 0.0) + pc[0] * R[m + 1][t - 1][u][w];
+                else if (u > 0) r = (u > 1 ? (u - 1) * R[m + 1][t][u - 2][w] : 0.0) + pc[1] * R[m + 1][t][u - 1][w];
+                else r = (w > 1 ? (w - 1) * R[m + 1][t][u][w - 2] : 0.0) + pc[2] * R[m + 1][t][u][w - 1];
+                R[m][t][u][w] = r;
+              }
+        const double pre = -P.charges[at] * 2.0 * pi / p * cc;
+        for (int i = 0; i < NA; ++i)
+          for (int j = 0; j < NB; ++j) {
+            const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
+            for (int d = 0; d < 3; ++d) {
+              double dV = 0.0;
+              for (int sgn = 0; sgn < 2; ++sgn) {
+                int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
+                const int ad = ax[d];
+                if (sgn == 1 && ad == 0) continue;
+                ax[d] += sgn == 0 ? 1 : -1;
+                const double f = sgn == 0 ? 2.0 * al : -(double)ad;
+                double acc = 0.0;
+                for (int t = 0; t <= ax[0] + bx[0]; ++t)
+                  for (int u = 0; u <= ax[1] + bx[1]; ++u)
+                    for (int w = 0; w <= ax[2] + bx[2]; ++w)
+                      acc += E[0][ax[0]][bx[0]][t] * E[1][ax[1]][bx[1]][u] * E[2][ax[2]][bx[2]][w] * R[0][t][u][w];
+                dV += f * acc;
+              }
+              const double v = Dab[i][j] * pre * dV;
+              gA[d] += v;
+              gC[d] -= v;
+            }
+          }
+      }
+    for (int d = 0; d < 3; ++d) atomicAdd(grad + 3 * at + d, 2.0 * gC[d]);
+  }
+  const int at_a = P.sh.atom[a];
+  for (int d = 0; d < 3; ++d) atomicAdd(grad + 3 * at_a + d, 2.0 * gA[d]);
+}
+
+__global__ void one_electron_grad_kernel(OneParams P, const double *D, const double *W, double *grad) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= P.nshell * P.nshell) return;
+  const int a = idx / P.nshell, b = idx % P.nshell;
+  switch (P.sh.l[a] * 3 + P.sh.l[b]) {
+    case 0: one_pair_grad<0, 0>(P, D, W, grad, a, b); break;
+    case 1: one_pair_grad<0, 1>(P, D, W, grad, a, b); break;
+    case 2: one_pair_grad<0, 2>(P, D, W, grad, a, b); break;
+    case 3: one_pair_grad<1, 0>(P, D, W, grad, a, b); break;
+    case 4: one_pair_grad<1, 1>(P, D, W, grad, a, b); break;
+    case 5: one_pair_grad<1, 2>(P, D, W, grad, a, b); break;
+    case 6: one_pair_grad<2, 0>(P, D, W, grad, a, b); break;
+    case 7: one_pair_grad<2, 1>(P, D, W, grad, a, b); break;
+    case 8: one_pair_grad<2, 2>(P, D, W, grad, a, b); break;
+    default: break;
+  }
+}
+
+cudaError_t launch_one_electron_grad(const OneParams &P, const double *D, const double *W, double *grad,
+                                     cudaStream_t st) {
+  const int n = P.nshell * P.nshell;
+  one_electron_grad_kernel<<<(n + 63) / 64, 64, 0, st>>>(P, D, W, grad);
+  return cudaGetLastError();
+}
+
 }  // namespace sf

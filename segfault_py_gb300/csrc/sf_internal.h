@@ -71,8 +71,9 @@ struct DevPairs {
 };
 
 // primitive-pair records (array of structures, 8 values each so that a
-// record is read with two vector loads in FP32 and three in FP64):
-//   [p, Px, Py, Pz, K~, 0.5/p, 0, 0]
+// record is read with two vector loads in FP32 and three in FP64; the
+// exponents alpha, beta of the two primitives are read only by gradients):
+//   [p, Px, Py, Pz, K~, 0.5/p, alpha, beta]
 constexpr int kPrimRec = 8;
 template <typename R>
 struct DevPrims {

@@ -74,7 +74,7 @@ def _density(F, X, norb):
     return 2.0 * Co @ Co.T, C, e
 
 
-def _run(mol, mode, tol, maxiter, precision, cutoff, fp32_cutoff, fb, device, damping=0.1, nbuffer=6):
+def _run(mol, mode, tol, maxiter, precision, cutoff, fp32_cutoff, fb, device, damping=0.1, nbuffer=6, dtol=None):
     fb, S, H, X = _setup(mol, fb, precision, cutoff, fp32_cutoff, device)
     norb = mol.nelectron // 2
     F = H.clone()
@@ -82,6 +82,7 @@ def _run(mol, mode, tol, maxiter, precision, cutoff, fp32_cutoff, fb, device, da
     counter = 0
     Fs, res, hist = [], [], []
     P_old = torch.zeros_like(H)
+    P_prev = None
     converged = False
     while True:
         P_new, C, eps = _density(F, X, norb)
@@ -94,7 +95,9 @@ def _run(mol, mode, tol, maxiter, precision, cutoff, fp32_cutoff, fb, device, da
         F = H + J - 0.5 * K
         etot = float(0.5 * torch.sum(P * (H + F)))
         hist.append(etot + mol.e_nuc)
-        if abs(etot - etot_old) <= tol:
+        dP = float(torch.sqrt(torch.mean((P - P_prev) ** 2))) if (dtol is not None and P_prev is not None) else 0.0
+        P_prev = P
+        if abs(etot - etot_old) <= tol and (dtol is None or dP <= dtol):
             converged = True
             break
         counter += 1
@@ -141,6 +144,7 @@ def scf_damping(mol: Molecule, tol=1e-8, maxiter=100, precision=None, cutoff=Non
 
 
 def scf_diis(mol: Molecule, tol=1e-8, maxiter=100, precision=None, cutoff=None,
-             fp32_cutoff=None, fb=None, device="cuda") -> SCFResult:
-    """hf.py:237-353 (Pulay cDIIS)."""
-    return _run(mol, "diis", tol, maxiter, precision, cutoff, fp32_cutoff, fb, device)
+             fp32_cutoff=None, fb=None, device="cuda", dtol=None) -> SCFResult:
+    """hf.py:237-353 (Pulay cDIIS).  ``dtol`` (not in the reference) also
+    requires the RMS density change to fall below it, as gradients need."""
+    return _run(mol, "diis", tol, maxiter, precision, cutoff, fp32_cutoff, fb, device, dtol=dtol)

@@ -120,3 +120,19 @@ def test_library_roots_vs_reference_root5():
     for x, res in zip(g["x"], g["res"]):
         L.sf_rys_roots_host(5, float(x), 0, u.ctypes.data, w.ctypes.data)
         np.testing.assert_allclose(np.concatenate([u, w]), res, rtol=2e-12)
+
+
+def test_nuclear_repulsion_gradient_fd():
+    from segfault_py_gb300.grad import nuclear_repulsion_gradient
+    from segfault_py_gb300.molecule import BOHR
+    s, x = G.water_cluster(2, seed=9)
+    m = Molecule.from_geometry(s, x, "sto-3g")
+    g = nuclear_repulsion_gradient(m)
+    h = 1e-5
+    for a in range(m.natom):
+        for d in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[a, d] += h * BOHR
+            xm[a, d] -= h * BOHR
+            fd = (Molecule.from_geometry(s, xp, "sto-3g").e_nuc - Molecule.from_geometry(s, xm, "sto-3g").e_nuc) / (2 * h)
+            assert abs(fd - g[a, d]) < 1e-7
