@@ -225,6 +225,9 @@ def run_ours(args):
     comb = (st_mx["flop_alg_fp64"] / (peaks["fp64"] * 1e12) + st_mx["flop_alg_fp32"] / (peaks["fp32"] * 1e12))
     build_frac = comb / (float(np.mean(t_mx)) * 1e-3)
     nn = mol.nao * mol.nao * 8
+    secondary = None
+    if args.nwater2 > 0:
+        secondary = secondary_config(args.nwater2, basis, max(5, args.steps // 2), args.warmup, flush, dev)
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(mol, args.cpu_seconds)
@@ -258,6 +261,7 @@ def run_ours(args):
                      "build_combined_frac": build_frac},
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "secondary": secondary,
     }
     print(json.dumps(rec))
     if world > 1:
@@ -265,6 +269,42 @@ def run_ours(args):
 
 
 # ----------------------------------------------------------------------------
+def secondary_config(nwater, basis, steps, warmup, flush, dev):
+    """Mixed vs FP64 Fock builds and forces on a second cluster size."""
+    import torch
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.grad import rhf_gradient
+    from segfault_py_gb300.scf import scf_diis
+    mol = workload(nwater, basis)
+    fb = FockBuilder(mol, device=dev, cutoff=CUTOFF, fp32_cutoff=FP32_CUTOFF, precision="mixed")
+    r = scf_diis(mol, tol=1e-9, fb=fb, device=dev, precision="fp64")
+    D, H = r.D.contiguous(), r.H
+    J, K = torch.empty_like(D), torch.empty_like(D)
+    stream = torch.cuda.current_stream()
+
+    def energy(prec):
+        fb.jk(D, precision=prec, out=(J, K))
+        return float(0.5 * torch.sum(D * (H + H + J - 0.5 * K)))
+    e64, emx = energy("fp64"), energy("mixed")
+    t = {p: time_steps(lambda: fb.jk(D, precision=p, out=(J, K)), steps, warmup, flush, stream)
+         for p in ("mixed", "fp64")}
+    tf = {p: time_steps(lambda: rhf_gradient(mol, r, fb, precision=p), max(3, steps // 4), warmup, flush, stream)
+          for p in ("mixed", "fp64")}
+    gerr = float((rhf_gradient(mol, r, fb, precision="mixed") - rhf_gradient(mol, r, fb, precision="fp64")).abs().max())
+    out = {"workload": "(H2O)%d water cluster, %s, seed 0" % (nwater, basis.upper()), "nao": mol.nao,
+           "fock_builds_per_s_mixed": 1e3 / float(np.mean(t["mixed"])),
+           "fock_builds_per_s_fp64": 1e3 / float(np.mean(t["fp64"])),
+           "mixed_speedup_vs_fp64": float(np.mean(t["fp64"])) / float(np.mean(t["mixed"])),
+           "forces_per_s_mixed": 1e3 / float(np.mean(tf["mixed"])),
+           "forces_per_s_fp64": 1e3 / float(np.mean(tf["fp64"])),
+           "mixed_fock_plus_forces_speedup_vs_fp64": (float(np.mean(t["fp64"])) + float(np.mean(tf["fp64"]))) /
+                                                     (float(np.mean(t["mixed"])) + float(np.mean(tf["mixed"]))),
+           "energy_error_mixed_vs_fp64": emx - e64, "max_grad_error_mixed_vs_fp64": gerr,
+           "scf_energy_fp64": r.energy}
+    fb.close()
+    return out
+
+
 def cpu_baseline(mol, seconds=15.0):
     """Oracle port of the reference algorithm on a bounded stride sample of the
     unique AO quartets (rows ij of the packed pair index with ij % stride == 0)."""
@@ -344,6 +384,7 @@ def main():
     ap.add_argument("--nwater", type=int, default=8)
     ap.add_argument("--basis", default="6-31g*")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nwater2", type=int, default=16, help="second cluster size reported beside (0: off)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -213,6 +213,13 @@ int sf_fma_peak(int32_t precision, double *flops, float *ms, void *stream);
 int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int32_t precision,
                        double cutoff, double fp32_cutoff, void *stream);
 
+/* x = A^-1 b for a small dense system (n <= 32; device row-major A[n*n],
+ * b[n], x[n]), Gaussian elimination with partial pivoting on the device;
+ * *ok (device double) = 1, or 0 with x = 0 when A is singular.  Used for the
+ * DIIS system (src/hf/hf.py:330-346) inside a captured SCF iteration, where a
+ * host-side check is not possible. */
+int sf_small_solve(int32_t n, const double *A, const double *b, double *x, double *ok, void *stream);
+
 /* Host evaluation of the library's Rys root table (for checks without a GPU):
  * n-point rule at x, u[i] = t_i^2, w[i] weights; fp32 != 0 selects the
  * single-precision table. */

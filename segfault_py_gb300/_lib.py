@@ -18,7 +18,8 @@ PRECISION = {"fp64": SF_PREC_FP64, "fp32": SF_PREC_FP32, "mixed": SF_PREC_MIXED}
 
 EXPORTS = ["sf_version", "sf_last_error", "sf_create", "sf_build_shells", "sf_destroy", "sf_nao", "sf_npairs",
            "sf_schwarz", "sf_fock_jk", "sf_set_partition", "sf_eri_batch", "sf_one_electron", "sf_rys_roots_host", "sf_set_profiling", "sf_slice_count", "sf_get_slice_info",
-           "sf_fma_peak", "sf_fock_jk_noalloc", "sf_grad_jk", "sf_grad_one_electron"]
+           "sf_fma_peak", "sf_fock_jk_noalloc", "sf_grad_jk", "sf_grad_one_electron",
+           "sf_small_solve"]
 
 
 class SegFockUnavailable(ImportError):
@@ -93,6 +94,7 @@ def lib():
     L.sf_fock_jk_noalloc.argtypes = [p, p, p, p, i32, d, d, p]
     L.sf_grad_jk.argtypes = [p, p, p, i32, d, d, p]
     L.sf_grad_one_electron.argtypes = [p, p, p, i32, p, p, p, p]
+    L.sf_small_solve.argtypes = [i32, p, p, p, p, p]
     _lib = L
     return L
 
