@@ -121,7 +121,7 @@ __global__ void to_float_kernel(const double *D, float *Df, int64_t n) {
 
 struct sf_handle {
   int device = 0;
-  int nshell = 0, nao = 0;
+  int nshell = 0, nao = 0, natom = 0;
   std::vector<int> l, nprim, atom, ao, spoff;
   std::vector<double> cx, cy, cz, exps, coefs;
   int cstart[kNumPairClass + 1] = {0};
@@ -180,6 +180,7 @@ void fill_kparams(sf_handle *h) {
   k.tab32 = h->d_tab32.p;
   k.asym = host_tables().asym;
   k.nao = h->nao;
+  k.natom = h->natom;
   k.err = h->d_err.p;
 }
 
@@ -476,6 +477,7 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
         return fail(SF_EINVAL, "sf_create: bad exponent/coefficient in shell " + std::to_string(s));
     for (int k = 0; k < 3; ++k)
       if (!std::isfinite(d.center[k])) return fail(SF_EINVAL, "sf_create: non-finite centre of shell " + std::to_string(s));
+    if (d.atom < 0) return fail(SF_EINVAL, "sf_create: negative atom index of shell " + std::to_string(s));
     ao += ncart(d.l);
   }
   sf_handle *h = new sf_handle();
@@ -501,6 +503,7 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
     nao += ncart(d.l);
   }
   h->nao = nao;
+  for (int s = 0; s < nshell; ++s) h->natom = std::max(h->natom, h->atom[s] + 1);
   // canonical shell pairs, grouped by pair class
   const double kpre = std::sqrt(2.0) * std::pow(3.14159265358979323846, 1.25);
   std::vector<double> pp[8];
@@ -801,11 +804,33 @@ int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, d
     to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, h->d_D32.p, (int64_t)nn);
     SF_CK(cudaGetLastError());
   }
-  return fan_out(h, st, [&](size_t k, cudaStream_t ss) {
+  auto launch = [&](size_t k, cudaStream_t ss) {
     const auto &s = h->slices[k];
     return s.prec == 0 ? launch_grad_f64(s.cls, h->kp, s.w, D, grad, ss)
                        : launch_grad_f32(s.cls, h->kp, s.w, h->d_D32.p, grad, ss);
-  });
+  };
+  if (h->profiling) {   // per-launch events (serialised in mode 2), read by sf_get_slice_info
+    while (h->ev.size() < 2 * h->slices.size()) {
+      cudaEvent_t e;
+      SF_CK(cudaEventCreate(&e));
+      h->ev.push_back(e);
+    }
+    if (h->profiling == 2) {
+      for (size_t k = 0; k < h->slices.size(); ++k) {
+        SF_CK(cudaEventRecord(h->ev[2 * k], st));
+        SF_CK(launch(k, st));
+        SF_CK(cudaEventRecord(h->ev[2 * k + 1], st));
+      }
+      return SF_OK;
+    }
+    return fan_out(h, st, [&](size_t k, cudaStream_t ss) {
+      cudaError_t e = cudaEventRecord(h->ev[2 * k], ss);
+      if (e == cudaSuccess) e = launch(k, ss);
+      if (e == cudaSuccess) e = cudaEventRecord(h->ev[2 * k + 1], ss);
+      return e;
+    });
+  }
+  return fan_out(h, st, launch);
 }
 
 int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *charges, int32_t natom, const double *D,
@@ -813,6 +838,9 @@ int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *cha
   if (!h) return fail(SF_EINVAL, "sf_grad_one_electron: NULL handle");
   if (!D || !W || !grad || natom < 0 || (natom > 0 && (!atom_xyz || !charges)))
     return fail(SF_EINVAL, "sf_grad_one_electron: bad arguments");
+  if (natom < h->natom)
+    return fail(SF_EINVAL, "sf_grad_one_electron: the shells reference atom " + std::to_string(h->natom - 1) +
+                               " but only " + std::to_string(natom) + " nuclei were given");
   DeviceGuard g(h->device);
   OneParams P;
   P.sh = h->kp.sh;

@@ -36,9 +36,10 @@ struct QG {
   }
 };
 
-// lanes per quartet of the gradient kernels (bigger tables than the energy)
+// lanes per quartet of the gradient kernels (bigger tables than the energy);
+// T = 1 keeps everything in registers
 __host__ __device__ constexpr int tgrad(int nabcd) {
-  return nabcd <= 3 ? 1 : nabcd <= 9 ? 2 : nabcd <= 27 ? 4 : nabcd <= 81 ? 8 : nabcd <= 216 ? 16 : 32;
+  return nabcd <= 18 ? 1 : nabcd <= 27 ? 4 : nabcd <= 81 ? 8 : nabcd <= 216 ? 16 : 32;
 }
 
 template <int LA, int LB, int LC, int LD, typename R, int T>
@@ -58,8 +59,106 @@ __device__ __forceinline__ void load_exps(const KParams &kp, int prim, R &e0, R 
   e1 = __ldg(rec + 1);
 }
 
+// T == 1: one lane per quartet, every table in registers, compile-time indices
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void grad_t1(const KParams &kp, const QGeom<R> &g, const R (&gam)[QC<LA, LB, LC, LD>::NABCD],
+                                        int p, int P, R (&gA)[3], R (&gB)[3], R (&gC)[3]) {
+  using Q = QC<LA, LB, LC, LD>;
+  using G = QG<LA, LB, LC, LD>;
+  constexpr int NR = G::NRG, SZ = G::SZE;
+  const int nprim = g.ab_n * g.cd_n;
+  int cur = -1;
+  PQ<R> s;
+  R pp, px, py, pz, kab, al = 0, be = 0;
+  for (int idx = p; idx < nprim; idx += P) {
+    const int ip = idx / g.cd_n, iq = idx - ip * g.cd_n;
+    if (ip != cur) {
+      load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
+      load_exps<R>(kp, g.ab_off + ip, al, be);
+      cur = ip;
+    }
+    load_prim_cd<R>(kp, g, iq, s, pp, px, py, pz, kab);
+    R ga, gd;
+    load_exps<R>(kp, g.cd_off + iq, ga, gd);
+    R u[NR], wr[NR];
+    rys_roots_all<NR, R>(kp, s.x, u, wr);
+    R sp[3][3], sm[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sp[c][d] = sm[c][d] = (R)0;
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      const R uu = u[r];
+      const R b00 = (R)0.5 * s.r2 * uu;
+      const R b10 = s.i2p * ((R)1 - s.aq * uu);
+      const R b01 = s.i2q * ((R)1 - s.ap * uu);
+      const R tq = s.aq * uu, tp = s.ap * uu;
+      R I[3][SZ];
+      rys_2d<LA + 1, LB + 1, LC + 1, LD, R>((R)1, s.pax - tq * s.pqx, s.qcx + tp * s.pqx, b00, b10, b01, g.ABx,
+                                            g.CDx, I[0]);
+      rys_2d<LA + 1, LB + 1, LC + 1, LD, R>((R)1, s.pay - tq * s.pqy, s.qcy + tp * s.pqy, b00, b10, b01, g.ABy,
+                                            g.CDy, I[1]);
+      rys_2d<LA + 1, LB + 1, LC + 1, LD, R>(s.pref * wr[r], s.paz - tq * s.pqz, s.qcz + tp * s.pqz, b00, b10, b01,
+                                            g.ABz, g.CDz, I[2]);
+#pragma unroll
+      for (int o = 0; o < Q::NABCD; ++o) {
+        const R ix = I[0][G::eoff(o, 0)], iy = I[1][G::eoff(o, 1)], iz = I[2][G::eoff(o, 2)];
+        const R wd[3] = {gam[o] * iy * iz, gam[o] * ix * iz, gam[o] * ix * iy};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int e = G::eoff(o, d);
+          const int ea = cart_e(LA, Q::ca(o), d), eb = cart_e(LB, Q::cb(o), d), ec = cart_e(LC, Q::cc(o), d);
+          sp[0][d] += wd[d] * I[d][e + G::SA];
+          sp[1][d] += wd[d] * I[d][e + G::SB];
+          sp[2][d] += wd[d] * I[d][e + G::SC];
+          if (ea) sm[0][d] += (R)ea * wd[d] * I[d][e - G::SA];
+          if (eb) sm[1][d] += (R)eb * wd[d] * I[d][e - G::SB];
+          if (ec) sm[2][d] += (R)ec * wd[d] * I[d][e - G::SC];
+        }
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      gA[d] += (R)2 * al * sp[0][d] - sm[0][d];
+      gB[d] += (R)2 * be * sp[1][d] - sm[1][d];
+      gC[d] += (R)2 * ga * sp[2][d] - sm[2][d];
+    }
+  }
+}
+
+template <int LA, int LB, int LC, int LD, typename R, int T>
+__device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork &w, const R *__restrict__ D,
+                                             double *grad, bool shared_acc);
+
+// Gradient contributions of a CTA are summed in shared memory (3 slots per
+// atom) and written with one atomic per slot at the end: all quartets add
+// into the same 3*natom words, so per-quartet global atomics serialise.
+constexpr int kGradSmemAtoms = 512;   // larger molecules add to global memory directly
+
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, const R *__restrict__ D, double *grad) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using GP0 = GGrp<LA, LB, LC, LD, R, T>;
+  const bool cta_sum = kp.natom <= kGradSmemAtoms;
+  double *sgrad = reinterpret_cast<double *>(smem_raw + (T == 1 ? 0 : (size_t)(kBlock / T) * GP0::BUFN * sizeof(R)));
+  if (cta_sum) {
+    for (int i = threadIdx.x; i < 3 * kp.natom; i += blockDim.x) sgrad[i] = 0.0;
+    __syncthreads();
+  }
+  const int TP0 = T * w.psplit;
+  const int64_t q0 = (int64_t)blockIdx.x * (kBlock / TP0) + threadIdx.x / TP0;
+  if (q0 < w.n) grad_quartet<LA, LB, LC, LD, R, T>(kp, w, D, cta_sum ? sgrad : grad, cta_sum);
+  if (cta_sum) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * kp.natom; i += blockDim.x)
+      if (sgrad[i] != 0.0) atomicAdd(grad + i, sgrad[i]);
+  }
+}
+
+template <int LA, int LB, int LC, int LD, typename R, int T>
+__device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork &w, const R *__restrict__ D,
+                                             double *grad, bool shared_acc) {
   using Q = QC<LA, LB, LC, LD>;
   using G = QG<LA, LB, LC, LD>;
   using GP = GGrp<LA, LB, LC, LD, R, T>;
@@ -68,7 +167,6 @@ __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, c
   const int TP = T * P;
   const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
   const int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp;
-  if (q >= w.n) return;
   const int2 ij = __ldg(w.list + q);
   const int pab = w.x0 + ij.x, pcd = w.y0 + ij.y;
   const QGeom<R> g = make_geom<R>(kp, pab, pcd, false, false);
@@ -81,6 +179,7 @@ __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, c
   const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R *tab = reinterpret_cast<R *>(smem_raw) + (threadIdx.x / T) * GP::BUFN;
+  (void)shared_acc;
 
   // G_o of this lane's outputs (normalised, permutation count folded in),
   // packed table offsets and Cartesian exponents of a, b, c per direction
@@ -106,6 +205,9 @@ __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, c
     }
   }
   R gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+  if constexpr (T == 1) {
+    grad_t1<LA, LB, LC, LD, R>(kp, g, gam, p, P, gA, gB, gC);
+  } else {
   const int nprim = g.ab_n * g.cd_n;
   int cur = -1;
   PQ<R> s;
@@ -183,6 +285,7 @@ __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, c
       gC[d] += (R)2 * ga * sp[2][d] - sm[2][d];
     }
   }
+  }
   // sum over the T x P lanes of the quartet
 #pragma unroll
   for (int d = 0; d < 3; ++d)
@@ -206,7 +309,8 @@ __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, c
 template <int LA, int LB, int LC, int LD, typename R>
 constexpr size_t grad_smem() {
   constexpr int T = tgrad(QC<LA, LB, LC, LD>::NABCD);
-  return (size_t)(kBlock / T) * GGrp<LA, LB, LC, LD, R, T>::BUFN * sizeof(R);
+  return (T == 1 ? 0 : (size_t)(kBlock / T) * GGrp<LA, LB, LC, LD, R, T>::BUFN * sizeof(R)) +
+         3 * kGradSmemAtoms * sizeof(double);
 }
 
 }  // namespace sf

@@ -210,7 +210,8 @@ cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st) {
 // -2 sum_ij D_ij <d phi_i/dA|1/r_C|phi_j>.
 // ---------------------------------------------------------------------------
 template <int LA, int LB>
-__device__ void one_pair_grad(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b) {
+__device__ void one_pair_grad(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b,
+                              int which) {
   constexpr int NA = ncart(LA), NB = ncart(LB);
   constexpr int LE = LA + 1;                 // bra shifted up by one
   constexpr int L = LA + LB + 1;
@@ -227,7 +228,9 @@ __device__ void one_pair_grad(const OneParams &P, const double *Dm, const double
     }
   double gA[3] = {0.0, 0.0, 0.0};
   double E[3][LE + 1][LB + 3][LE + LB + 3];
-  // overlap and kinetic: Pulay term -W dS and D dT
+  // which == natom: overlap and kinetic (Pulay term -W dS and D dT);
+  // which < natom: nuclear attraction of nucleus 'which'
+  if (which == P.natom)
   for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
     for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
       const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
@@ -264,8 +267,8 @@ __device__ void one_pair_grad(const OneParams &P, const double *Dm, const double
           }
         }
     }
-  // nuclear attraction, nucleus by nucleus
-  for (int at = 0; at < P.natom; ++at) {
+  // nuclear attraction of one nucleus
+  for (int at = which; at < P.natom && at == which; ++at) {
     const double Cc[3] = {P.atom_xyz[3 * at], P.atom_xyz[3 * at + 1], P.atom_xyz[3 * at + 2]};
     double gC[3] = {0.0, 0.0, 0.0};
     for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
@@ -329,28 +332,51 @@ __device__ void one_pair_grad(const OneParams &P, const double *Dm, const double
   for (int d = 0; d < 3; ++d) atomicAdd(grad + 3 * at_a + d, 2.0 * gA[d]);
 }
 
+// one thread per (ordered shell pair, nucleus or the S/T part); the
+// contributions of a CTA are summed in shared memory (3 slots per atom) and
+// written with one atomic per slot, because all threads add into the same
+// 3*natom words
+constexpr int kOneGradSmemAtoms = 512;
+
 __global__ void one_electron_grad_kernel(OneParams P, const double *D, const double *W, double *grad) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= P.nshell * P.nshell) return;
-  const int a = idx / P.nshell, b = idx % P.nshell;
-  switch (P.sh.l[a] * 3 + P.sh.l[b]) {
-    case 0: one_pair_grad<0, 0>(P, D, W, grad, a, b); break;
-    case 1: one_pair_grad<0, 1>(P, D, W, grad, a, b); break;
-    case 2: one_pair_grad<0, 2>(P, D, W, grad, a, b); break;
-    case 3: one_pair_grad<1, 0>(P, D, W, grad, a, b); break;
-    case 4: one_pair_grad<1, 1>(P, D, W, grad, a, b); break;
-    case 5: one_pair_grad<1, 2>(P, D, W, grad, a, b); break;
-    case 6: one_pair_grad<2, 0>(P, D, W, grad, a, b); break;
-    case 7: one_pair_grad<2, 1>(P, D, W, grad, a, b); break;
-    case 8: one_pair_grad<2, 2>(P, D, W, grad, a, b); break;
-    default: break;
+  extern __shared__ double sgrad[];
+  const bool cta_sum = P.natom <= kOneGradSmemAtoms;
+  if (cta_sum) {
+    for (int i = threadIdx.x; i < 3 * P.natom; i += blockDim.x) sgrad[i] = 0.0;
+    __syncthreads();
+  }
+  double *out = cta_sum ? sgrad : grad;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t npair = (int64_t)P.nshell * P.nshell;
+  if (idx < npair * (P.natom + 1)) {
+    const int which = (int)(idx / npair);
+    const int ab = (int)(idx % npair);
+    const int a = ab / P.nshell, b = ab % P.nshell;
+    switch (P.sh.l[a] * 3 + P.sh.l[b]) {
+      case 0: one_pair_grad<0, 0>(P, D, W, out, a, b, which); break;
+      case 1: one_pair_grad<0, 1>(P, D, W, out, a, b, which); break;
+      case 2: one_pair_grad<0, 2>(P, D, W, out, a, b, which); break;
+      case 3: one_pair_grad<1, 0>(P, D, W, out, a, b, which); break;
+      case 4: one_pair_grad<1, 1>(P, D, W, out, a, b, which); break;
+      case 5: one_pair_grad<1, 2>(P, D, W, out, a, b, which); break;
+      case 6: one_pair_grad<2, 0>(P, D, W, out, a, b, which); break;
+      case 7: one_pair_grad<2, 1>(P, D, W, out, a, b, which); break;
+      case 8: one_pair_grad<2, 2>(P, D, W, out, a, b, which); break;
+      default: break;
+    }
+  }
+  if (cta_sum) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * P.natom; i += blockDim.x)
+      if (sgrad[i] != 0.0) atomicAdd(grad + i, sgrad[i]);
   }
 }
 
 cudaError_t launch_one_electron_grad(const OneParams &P, const double *D, const double *W, double *grad,
                                      cudaStream_t st) {
-  const int n = P.nshell * P.nshell;
-  one_electron_grad_kernel<<<(n + 63) / 64, 64, 0, st>>>(P, D, W, grad);
+  const int64_t n = (int64_t)P.nshell * P.nshell * (P.natom + 1);
+  const size_t smem = P.natom <= kOneGradSmemAtoms ? 3 * (size_t)P.natom * sizeof(double) : 0;
+  one_electron_grad_kernel<<<(unsigned)((n + 127) / 128), 128, smem, st>>>(P, D, W, grad);
   return cudaGetLastError();
 }
 

@@ -38,6 +38,7 @@ struct KParams {
   const float *tab32;
   RysAsym asym;
   int nao;
+  int natom;           // atoms referenced by the shells (gradient length / 3)
   int *err;            // device error flag (unused by the arithmetic kernels)
 };
 

@@ -119,12 +119,12 @@ class GraphSCF:
         self.slot.copy_(torch.remainder(self.slot + use, float(NSLOT)))
         G = torch.einsum("iab,jab->ij", self.Rs, self.Rs)
         m = self.mask
-        mm = torch.outer(m, m)
-        Bm = G * mm + torch.diag(1.0 - m)
-        self.B[:NSLOT, :NSLOT] = Bm
-        self.B[:NSLOT, NSLOT] = -m
-        self.B[NSLOT, :NSLOT] = -m
-        self.B[NSLOT, NSLOT] = 0.0
+        Bm = G * torch.outer(m, m) + torch.diag(1.0 - m)
+        # bordered Pulay matrix assembled on the device (an item assignment of
+        # a Python number would copy from the host, which capture forbids)
+        top = torch.cat([Bm, -m.view(-1, 1)], dim=1)
+        bottom = torch.cat([-m.view(1, -1), torch.zeros(1, 1, dtype=m.dtype, device=m.device)], dim=1)
+        self.B.copy_(torch.cat([top, bottom], dim=0))
         _lib.check(L.sf_small_solve(NSLOT + 1, C.c_void_p(self.B.data_ptr()), C.c_void_p(self.rhs.data_ptr()),
                                     C.c_void_p(self.coef.data_ptr()), C.c_void_p(self.ok.data_ptr()),
                                     C.c_void_p(torch.cuda.current_stream().cuda_stream)))

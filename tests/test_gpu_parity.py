@@ -217,3 +217,25 @@ def test_mixed_precision_energy_error(cuda):
         return float(0.5 * torch.sum(D * (H + F)))
     e64, emx = energy("fp64"), energy("mixed")
     assert abs(emx - e64) < 1e-6
+
+
+def test_partition_slices_sum_to_full(cuda):
+    """sf_set_partition: the nparts slices of the quartet lists add up to the
+    full J/K (the multi-GPU sharding unit, run here one after another)."""
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.molecule import Molecule
+    s, x = G.water_cluster(3, seed=8)
+    mol = Molecule.from_geometry(s, x, "6-31g*")
+    D = torch.tensor(_rand_density(mol.nao, 4), device=cuda)
+    fb = _fb(mol)
+    J, K = fb.jk(D)
+    Js, Ks = torch.zeros_like(J), torch.zeros_like(K)
+    for part in range(3):
+        fb.set_partition(part, 3)
+        Jp, Kp = fb.jk(D)
+        Js += Jp
+        Ks += Kp
+    fb.set_partition(0, 1)
+    scale = float(max(J.abs().max(), K.abs().max()))
+    assert float((Js - J).abs().max()) < 1e-12 * scale
+    assert float((Ks - K).abs().max()) < 1e-12 * scale
