@@ -203,85 +203,118 @@ cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // Gradient of E1 = sum_ij D_ij (T_ij + V_ij) - W_ij S_ij.  With D, W and the
 // operators symmetric, d/dR sum_ij D_ij O_ij = 2 sum_ij D_ij <d phi_i/dR|O|phi_j>,
-// so one thread per ordered shell pair (a, b) differentiates the bra function
-// only, d phi_a / dA = 2 alpha phi_{a+1} - a phi_{a-1}, and counts it twice.
-// V also depends on the nucleus C: by translational invariance of
-// <a|1/r_C|b>, dV/dC = -(dV/dA + dV/dB), which over all ordered pairs is
-// -2 sum_ij D_ij <d phi_i/dA|1/r_C|phi_j>.
+// so only the bra function of each ordered shell pair is differentiated,
+// d phi_a / dA = 2 alpha phi_{a+1} - a phi_{a-1}, and counted twice.
 // ---------------------------------------------------------------------------
+// CTA per ordered shell pair (a, b), 64 threads.  For every primitive pair:
+//  * E coefficients (bra shifted to LA+1, ket to LB+2) into shared memory;
+//  * S and T bra-derivative terms (nucleus independent) by thread 0;
+//  * the density-contracted Hermite coefficients of the bra derivative,
+//      M^d_tuv = 2pi/p c_i c_j sum_{i in a, j in b} D_ij sum_+- f E^{i+-1_d, j}_t E_u E_v,
+//    cooperatively into shared memory (they do not depend on the nucleus);
+//  * every thread then takes nuclei C = t, t+64, ...: R_tuv(p, P - C) by the
+//    Hermite Coulomb recursion and dV/dA_d = -Z_C sum_tuv M^d_tuv R_tuv.
+// Each ordered pair counts twice (bra derivative of (a,b) = ket derivative of
+// (b,a)); the nucleus receives minus the basis-centre part (translational
+// invariance of <a|1/r_C|b>).
+constexpr int kOneGradThreads = 64;
+
 template <int LA, int LB>
-__device__ void one_pair_grad(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b,
-                              int which) {
+__device__ void one_pair_grad2(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b) {
   constexpr int NA = ncart(LA), NB = ncart(LB);
-  constexpr int LE = LA + 1;                 // bra shifted up by one
-  constexpr int L = LA + LB + 1;
+  constexpr int LE = LA + 1, L = LA + LB + 1, NH = (L + 1) * (L + 1) * (L + 1);
   const double pi = 3.14159265358979323846;
+  __shared__ double E[3][LE + 1][LB + 3][LE + LB + 3];
+  __shared__ double M[3][NH];
+  __shared__ double Dab[NA][NB];
+  __shared__ double red[kOneGradThreads][3];
+  const int tid = threadIdx.x;
   const double A[3] = {P.sh.cx[a], P.sh.cy[a], P.sh.cz[a]};
   const double B[3] = {P.sh.cx[b], P.sh.cy[b], P.sh.cz[b]};
   const int a0 = P.sh.ao[a], b0 = P.sh.ao[b], n = P.nao;
-  double Dab[NA][NB], Wab[NA][NB];
-  for (int i = 0; i < NA; ++i)
-    for (int j = 0; j < NB; ++j) {
-      const double nrm = cart_norm(LA, i) * cart_norm(LB, j);
-      Dab[i][j] = Dm[(a0 + i) * n + b0 + j] * nrm;
-      Wab[i][j] = Wm[(a0 + i) * n + b0 + j] * nrm;
-    }
+  for (int k = tid; k < NA * NB; k += blockDim.x) {
+    const int i = k / NB, j = k % NB;
+    Dab[i][j] = Dm[(a0 + i) * n + b0 + j] * cart_norm(LA, i) * cart_norm(LB, j);
+  }
   double gA[3] = {0.0, 0.0, 0.0};
-  double E[3][LE + 1][LB + 3][LE + LB + 3];
-  // which == natom: overlap and kinetic (Pulay term -W dS and D dT);
-  // which < natom: nuclear attraction of nucleus 'which'
-  if (which == P.natom)
   for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
     for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
       const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
       const double cc = P.coefs[ia] * P.coefs[ib];
-      for (int d = 0; d < 3; ++d) {
-        const double Pd = (al * A[d] + be * B[d]) / p, X = A[d] - B[d];
-        hermite_e<LE, LB + 2>(p, Pd - A[d], Pd - B[d], exp(-mu * X * X), E[d]);
+      double Pc[3];
+      for (int d = 0; d < 3; ++d) Pc[d] = (al * A[d] + be * B[d]) / p;
+      __syncthreads();   // previous iteration done with E, M
+      if (tid < 3) {
+        const int d = tid;
+        const double X = A[d] - B[d];
+        double Et[LE + 1][LB + 3][LE + LB + 3];
+        hermite_e<LE, LB + 2>(p, Pc[d] - A[d], Pc[d] - B[d], exp(-mu * X * X), Et);
+        for (int i = 0; i <= LE; ++i)
+          for (int j = 0; j <= LB + 2; ++j)
+            for (int t = 0; t <= LE + LB + 2; ++t) E[d][i][j][t] = Et[i][j][t];
       }
-      const double sp = pow(pi / p, 1.5);
-      for (int i = 0; i < NA; ++i)
-        for (int j = 0; j < NB; ++j) {
-          const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
-          for (int d = 0; d < 3; ++d) {
-            double dS = 0.0, dT = 0.0;
-            for (int sgn = 0; sgn < 2; ++sgn) {
-              int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
-              const int ad = ax[d];
-              if (sgn == 1 && ad == 0) continue;
-              ax[d] += sgn == 0 ? 1 : -1;
-              const double f = sgn == 0 ? 2.0 * al : -(double)ad;
-              const double sx = E[0][ax[0]][bx[0]][0], sy = E[1][ax[1]][bx[1]][0], sz = E[2][ax[2]][bx[2]][0];
-              const double s0 = sx * sy * sz * sp;
-              double t = be * (2 * (bx[0] + bx[1] + bx[2]) + 3) * s0;
-              t -= 2.0 * be * be * sp *
-                   (E[0][ax[0]][bx[0] + 2][0] * sy * sz + sx * E[1][ax[1]][bx[1] + 2][0] * sz +
-                    sx * sy * E[2][ax[2]][bx[2] + 2][0]);
-              if (bx[0] >= 2) t -= 0.5 * bx[0] * (bx[0] - 1) * sp * E[0][ax[0]][bx[0] - 2][0] * sy * sz;
-              if (bx[1] >= 2) t -= 0.5 * bx[1] * (bx[1] - 1) * sp * sx * E[1][ax[1]][bx[1] - 2][0] * sz;
-              if (bx[2] >= 2) t -= 0.5 * bx[2] * (bx[2] - 1) * sp * sx * sy * E[2][ax[2]][bx[2] - 2][0];
-              dS += f * s0;
-              dT += f * t;
+      __syncthreads();
+      // overlap / kinetic bra derivatives (Pulay -W dS, D dT)
+      if (tid == 0) {
+        const double sp = pow(pi / p, 1.5);
+        for (int i = 0; i < NA; ++i)
+          for (int j = 0; j < NB; ++j) {
+            const double nrm = cart_norm(LA, i) * cart_norm(LB, j);
+            const double Dij = Dab[i][j], Wij = Wm[(a0 + i) * n + b0 + j] * nrm;
+            const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
+            for (int d = 0; d < 3; ++d) {
+              double dS = 0.0, dT = 0.0;
+              for (int sgn = 0; sgn < 2; ++sgn) {
+                int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
+                const int ad = ax[d];
+                if (sgn == 1 && ad == 0) continue;
+                ax[d] += sgn == 0 ? 1 : -1;
+                const double f = sgn == 0 ? 2.0 * al : -(double)ad;
+                const double sx = E[0][ax[0]][bx[0]][0], sy = E[1][ax[1]][bx[1]][0], sz = E[2][ax[2]][bx[2]][0];
+                const double s0 = sx * sy * sz * sp;
+                double t = be * (2 * (bx[0] + bx[1] + bx[2]) + 3) * s0;
+                t -= 2.0 * be * be * sp *
+                     (E[0][ax[0]][bx[0] + 2][0] * sy * sz + sx * E[1][ax[1]][bx[1] + 2][0] * sz +
+                      sx * sy * E[2][ax[2]][bx[2] + 2][0]);
+                if (bx[0] >= 2) t -= 0.5 * bx[0] * (bx[0] - 1) * sp * E[0][ax[0]][bx[0] - 2][0] * sy * sz;
+                if (bx[1] >= 2) t -= 0.5 * bx[1] * (bx[1] - 1) * sp * sx * E[1][ax[1]][bx[1] - 2][0] * sz;
+                if (bx[2] >= 2) t -= 0.5 * bx[2] * (bx[2] - 1) * sp * sx * sy * E[2][ax[2]][bx[2] - 2][0];
+                dS += f * s0;
+                dT += f * t;
+              }
+              gA[d] += cc * (Dij * dT - Wij * dS);
             }
-            gA[d] += cc * (Dab[i][j] * dT - Wab[i][j] * dS);
           }
+      }
+      // density-contracted Hermite coefficients of the bra derivative
+      const double pre = 2.0 * pi / p * cc;
+      for (int k = tid; k < 3 * NH; k += blockDim.x) {
+        const int d = k / NH, h = k % NH;
+        const int t = h / ((L + 1) * (L + 1)), u = (h / (L + 1)) % (L + 1), v = h % (L + 1);
+        double m = 0.0;
+        if (t + u + v <= L) {
+          for (int i = 0; i < NA; ++i)
+            for (int j = 0; j < NB; ++j) {
+              const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
+              double acc = 0.0;
+              for (int sgn = 0; sgn < 2; ++sgn) {
+                int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
+                const int ad = ax[d];
+                if (sgn == 1 && ad == 0) continue;
+                ax[d] += sgn == 0 ? 1 : -1;
+                if (t > ax[0] + bx[0] || u > ax[1] + bx[1] || v > ax[2] + bx[2]) continue;
+                const double f = sgn == 0 ? 2.0 * al : -(double)ad;
+                acc += f * E[0][ax[0]][bx[0]][t] * E[1][ax[1]][bx[1]][u] * E[2][ax[2]][bx[2]][v];
+              }
+              m += Dab[i][j] * acc;
+            }
         }
-    }
-  // nuclear attraction of one nucleus
-  for (int at = which; at < P.natom && at == which; ++at) {
-    const double Cc[3] = {P.atom_xyz[3 * at], P.atom_xyz[3 * at + 1], P.atom_xyz[3 * at + 2]};
-    double gC[3] = {0.0, 0.0, 0.0};
-    for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
-      for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
-        const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
-        const double cc = P.coefs[ia] * P.coefs[ib];
-        double Pc[3];
-        for (int d = 0; d < 3; ++d) {
-          Pc[d] = (al * A[d] + be * B[d]) / p;
-          const double X = A[d] - B[d];
-          hermite_e<LE, LB + 2>(p, Pc[d] - A[d], Pc[d] - B[d], exp(-mu * X * X), E[d]);
-        }
-        const double pc[3] = {Pc[0] - Cc[0], Pc[1] - Cc[1], Pc[2] - Cc[2]};
+        M[d][h] = pre * m;
+      }
+      __syncthreads();
+      for (int at = tid; at < P.natom; at += blockDim.x) {
+        const double pc[3] = {Pc[0] - P.atom_xyz[3 * at], Pc[1] - P.atom_xyz[3 * at + 1],
+                              Pc[2] - P.atom_xyz[3 * at + 2]};
         double F[L + 1];
         boys_array(L, p * (pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]), F);
         double R[L + 1][L + 1][L + 1][L + 1];
@@ -301,82 +334,54 @@ __device__ void one_pair_grad(const OneParams &P, const double *Dm, const double
                 else r = (w > 1 ? (w - 1) * R[m + 1][t][u][w - 2] : 0.0) + pc[2] * R[m + 1][t][u][w - 1];
                 R[m][t][u][w] = r;
               }
-        const double pre = -P.charges[at] * 2.0 * pi / p * cc;
-        for (int i = 0; i < NA; ++i)
-          for (int j = 0; j < NB; ++j) {
-            const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
-            for (int d = 0; d < 3; ++d) {
-              double dV = 0.0;
-              for (int sgn = 0; sgn < 2; ++sgn) {
-                int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
-                const int ad = ax[d];
-                if (sgn == 1 && ad == 0) continue;
-                ax[d] += sgn == 0 ? 1 : -1;
-                const double f = sgn == 0 ? 2.0 * al : -(double)ad;
-                double acc = 0.0;
-                for (int t = 0; t <= ax[0] + bx[0]; ++t)
-                  for (int u = 0; u <= ax[1] + bx[1]; ++u)
-                    for (int w = 0; w <= ax[2] + bx[2]; ++w)
-                      acc += E[0][ax[0]][bx[0]][t] * E[1][ax[1]][bx[1]][u] * E[2][ax[2]][bx[2]][w] * R[0][t][u][w];
-                dV += f * acc;
-              }
-              const double v = Dab[i][j] * pre * dV;
-              gA[d] += v;
-              gC[d] -= v;
+        double dv[3] = {0.0, 0.0, 0.0};
+        for (int t = 0; t <= L; ++t)
+          for (int u = 0; u <= L - t; ++u)
+            for (int w = 0; w <= L - t - u; ++w) {
+              const int h = (t * (L + 1) + u) * (L + 1) + w;
+              const double rr = R[0][t][u][w];
+              dv[0] += M[0][h] * rr;
+              dv[1] += M[1][h] * rr;
+              dv[2] += M[2][h] * rr;
             }
-          }
+        const double z = -P.charges[at];
+        for (int d = 0; d < 3; ++d) {
+          gA[d] += z * dv[d];
+          atomicAdd(grad + 3 * at + d, -2.0 * z * dv[d]);
+        }
       }
-    for (int d = 0; d < 3; ++d) atomicAdd(grad + 3 * at + d, 2.0 * gC[d]);
+    }
+  // reduce gA over the CTA, one atomic per direction
+  for (int d = 0; d < 3; ++d) red[tid][d] = gA[d];
+  __syncthreads();
+  if (tid < 3) {
+    double sacc = 0.0;
+    for (int k = 0; k < (int)blockDim.x; ++k) sacc += red[k][tid];
+    atomicAdd(grad + 3 * P.sh.atom[a] + tid, 2.0 * sacc);
   }
-  const int at_a = P.sh.atom[a];
-  for (int d = 0; d < 3; ++d) atomicAdd(grad + 3 * at_a + d, 2.0 * gA[d]);
 }
 
-// one thread per (ordered shell pair, nucleus or the S/T part); the
-// contributions of a CTA are summed in shared memory (3 slots per atom) and
-// written with one atomic per slot, because all threads add into the same
-// 3*natom words
-constexpr int kOneGradSmemAtoms = 512;
-
-__global__ void one_electron_grad_kernel(OneParams P, const double *D, const double *W, double *grad) {
-  extern __shared__ double sgrad[];
-  const bool cta_sum = P.natom <= kOneGradSmemAtoms;
-  if (cta_sum) {
-    for (int i = threadIdx.x; i < 3 * P.natom; i += blockDim.x) sgrad[i] = 0.0;
-    __syncthreads();
-  }
-  double *out = cta_sum ? sgrad : grad;
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t npair = (int64_t)P.nshell * P.nshell;
-  if (idx < npair * (P.natom + 1)) {
-    const int which = (int)(idx / npair);
-    const int ab = (int)(idx % npair);
-    const int a = ab / P.nshell, b = ab % P.nshell;
-    switch (P.sh.l[a] * 3 + P.sh.l[b]) {
-      case 0: one_pair_grad<0, 0>(P, D, W, out, a, b, which); break;
-      case 1: one_pair_grad<0, 1>(P, D, W, out, a, b, which); break;
-      case 2: one_pair_grad<0, 2>(P, D, W, out, a, b, which); break;
-      case 3: one_pair_grad<1, 0>(P, D, W, out, a, b, which); break;
-      case 4: one_pair_grad<1, 1>(P, D, W, out, a, b, which); break;
-      case 5: one_pair_grad<1, 2>(P, D, W, out, a, b, which); break;
-      case 6: one_pair_grad<2, 0>(P, D, W, out, a, b, which); break;
-      case 7: one_pair_grad<2, 1>(P, D, W, out, a, b, which); break;
-      case 8: one_pair_grad<2, 2>(P, D, W, out, a, b, which); break;
-      default: break;
-    }
-  }
-  if (cta_sum) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < 3 * P.natom; i += blockDim.x)
-      if (sgrad[i] != 0.0) atomicAdd(grad + i, sgrad[i]);
+__global__ void __launch_bounds__(kOneGradThreads) one_electron_grad_kernel(OneParams P, const double *D,
+                                                                            const double *W, double *grad) {
+  const int a = blockIdx.x / P.nshell, b = blockIdx.x % P.nshell;
+  switch (P.sh.l[a] * 3 + P.sh.l[b]) {
+    case 0: one_pair_grad2<0, 0>(P, D, W, grad, a, b); break;
+    case 1: one_pair_grad2<0, 1>(P, D, W, grad, a, b); break;
+    case 2: one_pair_grad2<0, 2>(P, D, W, grad, a, b); break;
+    case 3: one_pair_grad2<1, 0>(P, D, W, grad, a, b); break;
+    case 4: one_pair_grad2<1, 1>(P, D, W, grad, a, b); break;
+    case 5: one_pair_grad2<1, 2>(P, D, W, grad, a, b); break;
+    case 6: one_pair_grad2<2, 0>(P, D, W, grad, a, b); break;
+    case 7: one_pair_grad2<2, 1>(P, D, W, grad, a, b); break;
+    case 8: one_pair_grad2<2, 2>(P, D, W, grad, a, b); break;
+    default: break;
   }
 }
 
 cudaError_t launch_one_electron_grad(const OneParams &P, const double *D, const double *W, double *grad,
                                      cudaStream_t st) {
-  const int64_t n = (int64_t)P.nshell * P.nshell * (P.natom + 1);
-  const size_t smem = P.natom <= kOneGradSmemAtoms ? 3 * (size_t)P.natom * sizeof(double) : 0;
-  one_electron_grad_kernel<<<(unsigned)((n + 127) / 128), 128, smem, st>>>(P, D, W, grad);
+  const int n = P.nshell * P.nshell;
+  one_electron_grad_kernel<<<n, kOneGradThreads, 0, st>>>(P, D, W, grad);
   return cudaGetLastError();
 }
 

@@ -137,6 +137,19 @@ class FockBuilder:
             self.last_stats = st.as_dict()
         return J, K
 
+    def capture_jk(self, D: torch.Tensor, J: torch.Tensor, K: torch.Tensor, precision: str | None = None):
+        """Capture one Fock build J, K = jk(D) on these static tensors as a CUDA
+        graph (the class launches and their stream fork/join become graph
+        nodes); returns the graph -- ``g.replay()`` rebuilds J and K for the
+        current contents of D without any host-side launch work."""
+        self.jk(D, precision=precision, out=(J, K))          # builds the quartet lists (allocates)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.jk(D, precision=precision, out=(J, K))
+        torch.cuda.synchronize()
+        return g
+
     def set_profiling(self, on=True):
         """True/1: time every class launch; 2: also serialise the launches on
         the caller's stream so each time is the kernel alone."""
