@@ -1,5 +1,7 @@
 // classes.h -- the 21 canonical shell-quartet classes (la lb | lc ld) with
-// l <= 2 and the thread-group size T used for each.  Class id = X(X+1)/2 + Y
+// l <= 2 and the thread-group size T used for each.  T = 1 keeps the quartet
+// in registers; FP32 needs half the registers of FP64, so classes up to 81
+// Cartesian outputs stay register-resident in FP32.  Class id = X(X+1)/2 + Y
 // for pair classes X >= Y (ss=0 ps=1 pp=2 ds=3 dp=4 dd=5).
 //   X(id, la, lb, lc, ld, T_fp64, T_fp32)
 #pragma once
@@ -9,17 +11,17 @@
   X(2, 1, 0, 1, 0, 1, 1)       \
   X(3, 1, 1, 0, 0, 1, 1)       \
   X(4, 1, 1, 1, 0, 1, 1)       \
-  X(5, 1, 1, 1, 1, 4, 4)       \
+  X(5, 1, 1, 1, 1, 4, 1)       \
   X(6, 2, 0, 0, 0, 1, 1)       \
   X(7, 2, 0, 1, 0, 1, 1)       \
-  X(8, 2, 0, 1, 1, 2, 2)       \
-  X(9, 2, 0, 2, 0, 2, 2)       \
+  X(8, 2, 0, 1, 1, 2, 1)       \
+  X(9, 2, 0, 2, 0, 2, 1)       \
   X(10, 2, 1, 0, 0, 1, 1)      \
-  X(11, 2, 1, 1, 0, 2, 2)      \
+  X(11, 2, 1, 1, 0, 2, 1)      \
   X(12, 2, 1, 1, 1, 8, 8)      \
   X(13, 2, 1, 2, 0, 4, 4)      \
   X(14, 2, 1, 2, 1, 16, 16)    \
-  X(15, 2, 2, 0, 0, 2, 2)      \
+  X(15, 2, 2, 0, 0, 2, 1)      \
   X(16, 2, 2, 1, 0, 4, 4)      \
   X(17, 2, 2, 1, 1, 16, 16)    \
   X(18, 2, 2, 2, 0, 8, 8)      \
