@@ -9,8 +9,8 @@ einsums of the reference's hf.py:300 without the N^4 tensor), mixed precision.
 Reported:
 * value        Fock builds/s, mixed path, D/J/K resident in HBM; L2 flushed
                (256 MB write) before every step, each step timed by CUDA events;
-               each build is one CUDA-graph replay of the library's class
-               launches (eager_launch_value: the same build launched eagerly)
+               each build launched eagerly through FockBuilder.jk
+               (graph_replay_value: the same build replayed from a CUDA graph)
 * e2e          same metric through the public API with host buffers: pinned D
                -> device, Fock build, J and K -> pinned host, every step
 * fp64         the all-FP64 build, same protocol (the plain FP64 GPU baseline)

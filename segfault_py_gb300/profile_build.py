@@ -1,0 +1,76 @@
+"""Per-launch device times of one Fock build.
+
+    python -m segfault_py_gb300.profile_build --nwater 8 --precision mixed --fp32-cutoff 1e-2
+
+Builds the seeded water cluster (6-31G* by default), forms the core-Hamiltonian
+guess density (the work of a build does not depend on the density values, only
+on the Schwarz bounds) and runs `--builds` Fock builds.  With `--slices` the
+library serialises its launches on one stream and times each with CUDA events;
+the table lists, per launch (one class, precision and lanes-per-quartet
+segment), the quartets, primitive quartets, device time, share of the build
+and algorithmic GFLOP/s.  Without `--slices` it only runs the builds (the
+command to put under a profiler).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import torch
+
+from . import geometry
+from .fock import FockBuilder
+from .molecule import Molecule
+from .scf import preload_torch_linalg
+
+
+def guess_density(fb: FockBuilder, nocc: int) -> torch.Tensor:
+    S, T, V = fb.one_electron()
+    w, U = torch.linalg.eigh(S)
+    X = U @ torch.diag(w.rsqrt()) @ U.T
+    _, Cp = torch.linalg.eigh(X @ (T + V) @ X)
+    C = (X @ Cp)[:, :nocc]
+    return 2.0 * C @ C.T
+
+
+def slice_table(fb: FockBuilder):
+    sl = fb.slice_info()
+    tot = sum(q["ms"] for q in sl)
+    rows = []
+    for q in sorted(sl, key=lambda q: -q["ms"]):
+        rows.append("(%d%d|%d%d) %s T=%2d q=%9d pq=%11d ms=%8.4f share=%5.1f%% GF/s=%8.1f" % (
+            q["la"], q["lb"], q["lc"], q["ld"], "f64" if q["precision"] == 0 else "f32",
+            q["threads_per_quartet"], q["quartets"], q["prim_quartets"], q["ms"],
+            100.0 * q["ms"] / max(tot, 1e-30), q["flop_alg"] / max(q["ms"], 1e-30) / 1e6))
+    return tot, rows
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nwater", type=int, default=8)
+    ap.add_argument("--basis", default="6-31g*")
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "fp32", "mixed"])
+    ap.add_argument("--cutoff", type=float, default=1e-12)
+    ap.add_argument("--fp32-cutoff", type=float, default=1e-2)
+    ap.add_argument("--builds", type=int, default=3)
+    ap.add_argument("--slices", action="store_true")
+    a = ap.parse_args(argv)
+    preload_torch_linalg()
+    sym, xyz = geometry.water_cluster(a.nwater)
+    mol = Molecule.from_geometry(sym, xyz, a.basis)
+    fb = FockBuilder(mol, cutoff=a.cutoff, fp32_cutoff=a.fp32_cutoff, precision=a.precision)
+    D = guess_density(fb, mol.nelectron // 2)
+    if a.slices:
+        fb.set_profiling(2)
+    for _ in range(a.builds):
+        fb.jk(D, stats=True)
+    torch.cuda.synchronize()
+    print("== %s nao=%d builds=%d stats %s" % (a.precision, fb.nao, a.builds, json.dumps(fb.last_stats)))
+    if a.slices:
+        tot, rows = slice_table(fb)
+        print("serialised kernel time of one build: %.4f ms" % tot)
+        print("\n".join(rows))
+
+
+if __name__ == "__main__":
+    main()
