@@ -20,6 +20,9 @@ Reported:
                per unique AO quartet, 5 Rys roots, no screening, OpenMP over
                all host cores) on a bounded stride sample, extrapolated
 * clocks       nvidia-smi samples taken during the timed region
+* secondary    (H2O)16 6-31G*: mixed vs FP64 Fock builds/s and forces/s
+* eri_batch    1e6 random shell quartets over all 21 classes: raw-ERI
+               quartets/s in FP64 and FP32 through one prepared plan
 
 ``--impl reference`` times the reference's CPU algorithm (oracle port, all host
 cores) on the same workload and prints the same metric.
@@ -233,6 +236,9 @@ def run_ours(args):
     secondary = None
     if args.nwater2 > 0:
         secondary = secondary_config(args.nwater2, basis, max(5, args.steps // 2), args.warmup, flush, dev)
+    eri = None
+    if args.eri_quartets > 0:
+        eri = eri_batch_config(args.eri_quartets, 3, args.warmup, flush, dev, peaks)
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(mol, args.cpu_seconds)
@@ -268,6 +274,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
         "secondary": secondary,
+        "eri_batch": eri,
     }
     print(json.dumps(rec))
     if world > 1:
@@ -309,6 +316,39 @@ def secondary_config(nwater, basis, steps, warmup, flush, dev):
            "scf_energy_fp64": r.energy}
     fb.close()
     return out
+
+
+def eri_batch_config(nq, steps, warmup, flush, dev, peaks):
+    """Raw-ERI stress batch: nq random contracted shell quartets, class
+    uniform over ss|ss .. dd|dd, contraction 1-6, exponents log-uniform in
+    [0.05, 1e4], centres in a 10 A box (seed 0); one prepared plan, every class
+    launched on the side streams; FP64 and FP32 outputs (stored as float64)."""
+    import torch
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    table, q = G.random_quartet_batch(nq, seed=0)
+    fb = FockBuilder(table, device=dev)
+    plan = fb.eri_plan(q)
+    stream = torch.cuda.current_stream()
+    out64 = torch.empty(plan.outputs, dtype=torch.float64, device=dev)
+    out32 = torch.empty_like(out64)
+    t = {"fp64": time_steps(lambda: plan.run("fp64", out64), steps, warmup, flush, stream),
+         "fp32": time_steps(lambda: plan.run("fp32", out32), steps, warmup, flush, stream)}
+    diff = float((out32 - out64).abs().max())
+    amax = float(out64.abs().max())
+    res = {"workload": "%d random contracted shell quartets, classes ss|ss..dd|dd uniform, K 1-6, "
+                       "exponents log-uniform [0.05, 1e4], 10 A box, seed 0" % nq,
+           "outputs": plan.outputs, "prim_quartets": plan.prim_quartets, "flop_alg": plan.flop_alg}
+    for p in ("fp64", "fp32"):
+        ms = float(np.mean(t[p]))
+        res[p] = {"ms": ms, "quartets_per_s": nq / (ms * 1e-3), "prim_quartets_per_s": plan.prim_quartets / (ms * 1e-3),
+                  "tflops_alg": plan.flop_alg / (ms * 1e-3) / 1e12,
+                  "frac_of_fma_peak": plan.flop_alg / (ms * 1e-3) / 1e12 / peaks[p] if peaks.get(p) else None}
+    res["max_abs_diff_fp32_vs_fp64"] = diff
+    res["max_abs_fp64"] = amax
+    plan.close()
+    fb.close()
+    return res
 
 
 def cpu_baseline(mol, seconds=15.0):
@@ -392,6 +432,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nwater2", type=int, default=16, help="second cluster size reported beside (0: off)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--eri-quartets", type=int, default=1_000_000, help="raw-ERI stress batch size (0: off)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

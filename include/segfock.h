@@ -53,6 +53,11 @@ extern "C" {
 #define SF_PREC_FP64 0      /* every quartet in FP64                          */
 #define SF_PREC_FP32 1      /* every quartet in FP32 (FP64 accumulation)      */
 #define SF_PREC_MIXED 2     /* FP64 above the FP32 cutoff, FP32 below it      */
+#define SF_PREC_MIXED_DF 3  /* double-float (FP32 pairs, ~2^-44 relative) above
+                               the FP32 cutoff, FP32 below it                 */
+#define SF_PREC_DF 4        /* every quartet in double-float                  */
+/* kind of one launch (sf_slice_info.precision, sf_tune_entry.precision):
+ * 0 FP64, 1 FP32, 2 double-float */
 
 typedef struct sf_handle sf_handle;
 
@@ -114,13 +119,41 @@ int sf_schwarz(sf_handle *h, double *q_out, void *stream);
 /* Coulomb and exchange matrices for a symmetric density D (device, nao*nao):
  *   J_pq = sum_rs (pq|rs) D_rs,  K_pq = sum_rs (pr|qs) D_rs
  * (the two einsums of src/hf/hf.py:300), over the canonical shell quartets
- * with Q_ab Q_cd >= cutoff.  In SF_PREC_MIXED, quartets with
- * Q_ab Q_cd < fp32_cutoff are evaluated in FP32; J and K are accumulated in
- * FP64 in every mode.  J, K: device, nao*nao, overwritten.
+ * with Q_ab Q_cd >= cutoff.  In SF_PREC_MIXED and SF_PREC_MIXED_DF, quartets
+ * with Q_ab Q_cd < fp32_cutoff are evaluated in FP32, the others in FP64
+ * (MIXED) or double-float (MIXED_DF); J and K are accumulated in FP64 in
+ * every mode.  sf_stats counts the FP64 / double-float tier as "fp64".
+ * J, K: device, nao*nao, overwritten.
  * stats (optional, host) receives counters.  Does not synchronise unless
  * stats is given. */
 int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t precision,
                double cutoff, double fp32_cutoff, sf_stats *stats, void *stream);
+
+/* Autotuner of the launch shapes.  Each launch of a Fock build (one class,
+ * one precision, one cost segment of the quartet list) maps a quartet onto
+ * T x P x W lanes: T lanes share its Cartesian outputs (fixed per class),
+ * its primitive loop is split S = P*W ways (P lane groups inside a warp, W
+ * separate groups whose partial integrals are digested separately).  The
+ * library picks S by a cost rule; sf_autotune times, for every launch of the
+ * given precision and cutoffs, S/4, S/2, S, 2S, 4S on `stream` (each candidate
+ * reps times, launches serialised, adding into the handle's scratch only),
+ * keeps the fastest and records it; later builds with the same work lists use
+ * the recorded splits.  Returns the number of launches tuned (>= 0) or an
+ * error code.  The table can be read out and loaded again (e.g. from a file):
+ * sf_set_tuning replaces it (n = 0 clears it). */
+typedef struct {
+    int32_t cls;           /* canonical class 0..20 (ss|ss .. dd|dd)          */
+    int32_t precision;     /* launch kind: 0 FP64, 1 FP32, 2 double-float     */
+    int64_t cost;          /* K_ab*K_cd of the launch's first (costliest) quartet */
+    int32_t split;         /* chosen S = P*W (power of two)                   */
+    float ms_default;      /* measured time with the rule's S                 */
+    float ms_tuned;        /* measured time with the chosen S                 */
+} sf_tune_entry;
+int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff, double fp32_cutoff,
+                int32_t reps, void *stream);
+int32_t sf_tuning_count(const sf_handle *h);
+int sf_get_tuning(const sf_handle *h, int32_t idx, sf_tune_entry *out);
+int sf_set_tuning(sf_handle *h, const sf_tune_entry *entries, int32_t n);
 
 /* Restrict sf_fock_jk to the slice [part, part+1) of nparts equal-work slices
  * of every quartet class (replica / multi-GPU partitioning hook; 0,1 = all). */
@@ -129,10 +162,29 @@ int sf_set_partition(sf_handle *h, int32_t part, int32_t nparts);
 /* Raw contracted ERIs of nq shell quartets (device int32[nq*4] shell ids, any
  * order of angular momenta).  out (device) receives, for quartet q at
  * out_offsets[q] (device int64[nq]), the ncart(a)*ncart(b)*ncart(c)*ncart(d)
- * integrals (ab|cd) in row-major component order.  precision: SF_PREC_FP64 or
- * SF_PREC_FP32 (FP32 evaluation, stored as double). */
+ * integrals (ab|cd) in row-major component order.  precision: SF_PREC_FP64,
+ * SF_PREC_FP32 or SF_PREC_DF (evaluated in that arithmetic, stored as
+ * double). */
 int sf_eri_batch(sf_handle *h, const int32_t *quartets, int64_t nq, int32_t precision,
                  double *out, const int64_t *out_offsets, void *stream);
+
+/* The same raw-ERI batch prepared once and run many times (replaces the
+ * per-AO-quartet rys.eri_rys calls of src/hf/hf.py:26-30 as one batched
+ * evaluation).  sf_eri_plan_create takes the shell quartets on the HOST
+ * (int32[nq*4]); the plan owns the class-sorted device work lists; outputs are
+ * packed in input order (quartet q at offsets[q], ncart(a)*ncart(b)*ncart(c)*
+ * ncart(d) values, row-major).  sf_eri_plan_run launches every class on the
+ * handle's side streams, forked from and joined back into `stream`; it
+ * allocates nothing and can be captured in a CUDA graph.  A plan belongs to
+ * its handle and must be destroyed before it. */
+typedef struct sf_eri_plan sf_eri_plan;
+int sf_eri_plan_create(sf_handle *h, const int32_t *quartets, int64_t nq, sf_eri_plan **out);
+/* total output doubles, primitive quartets and algorithmic FLOPs of one run */
+int sf_eri_plan_info(const sf_eri_plan *plan, int64_t *outputs, int64_t *prim_quartets, double *flop_alg);
+/* host int64[nq]: output offset of every quartet */
+int sf_eri_plan_offsets(const sf_eri_plan *plan, int64_t *offsets);
+int sf_eri_plan_run(sf_eri_plan *plan, int32_t precision, double *out, void *stream);
+void sf_eri_plan_destroy(sf_eri_plan *plan);
 
 /* One-electron matrices (device, nao*nao each): overlap S, kinetic T and
  * nuclear attraction V = sum_C -Z_C <a|1/r_C|b> for natom point charges
@@ -146,8 +198,10 @@ int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges,
  *   grad[3*A + d] += sum_{pqrs} G_pqrs d(pq|rs)/dR_{A,d},
  *   G_pqrs = 1/2 D_pq D_rs - 1/8 (D_pr D_qs + D_ps D_qr),
  * i.e. the derivative of 1/2 sum_pq D_pq (J - K/2)_pq at fixed D, over the
- * same screened quartets and precision split as sf_fock_jk.  grad (device,
- * 3 doubles per atom index used by the shells) is accumulated, not zeroed. */
+ * same screened quartets and precision split as sf_fock_jk (the derivative
+ * kernels exist in FP64 and FP32: SF_PREC_MIXED_DF runs as SF_PREC_MIXED and
+ * SF_PREC_DF as SF_PREC_FP64).  grad (device, 3 doubles per atom index used
+ * by the shells) is accumulated, not zeroed. */
 int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, double cutoff,
                double fp32_cutoff, void *stream);
 
@@ -169,13 +223,13 @@ int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *cha
  * src/hf/utils.py:76-83). */
 typedef struct {
     int32_t cls;              /* canonical class id 0..20                      */
-    int32_t precision;        /* SF_PREC_FP64 or SF_PREC_FP32                 */
+    int32_t precision;        /* launch kind: 0 FP64, 1 FP32, 2 double-float   */
     int32_t la, lb, lc, ld;
     int64_t quartets;
     int64_t prim_quartets;
     double flop_alg;
     float ms;                 /* device time of the last profiled launch      */
-    int32_t threads_per_quartet;   /* lanes per quartet: Cartesian split x primitive split */
+    int32_t threads_per_quartet;   /* lanes per quartet: Cartesian split T x primitive split (P lane groups x W groups) */
 } sf_slice_info;
 
 int sf_set_profiling(sf_handle *h, int32_t on);

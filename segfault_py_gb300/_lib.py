@@ -14,12 +14,16 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "lib
 SF_PREC_FP64 = 0
 SF_PREC_FP32 = 1
 SF_PREC_MIXED = 2
-PRECISION = {"fp64": SF_PREC_FP64, "fp32": SF_PREC_FP32, "mixed": SF_PREC_MIXED}
+SF_PREC_MIXED_DF = 3
+SF_PREC_DF = 4
+PRECISION = {"fp64": SF_PREC_FP64, "fp32": SF_PREC_FP32, "mixed": SF_PREC_MIXED, "mixed_df": SF_PREC_MIXED_DF,
+             "df": SF_PREC_DF}
 
 EXPORTS = ["sf_version", "sf_last_error", "sf_create", "sf_build_shells", "sf_destroy", "sf_nao", "sf_npairs",
            "sf_schwarz", "sf_fock_jk", "sf_set_partition", "sf_eri_batch", "sf_one_electron", "sf_rys_roots_host", "sf_set_profiling", "sf_slice_count", "sf_get_slice_info",
            "sf_fma_peak", "sf_fock_jk_noalloc", "sf_grad_jk", "sf_grad_one_electron",
-           "sf_small_solve"]
+           "sf_small_solve", "sf_eri_plan_create", "sf_eri_plan_info", "sf_eri_plan_offsets", "sf_eri_plan_run",
+           "sf_eri_plan_destroy", "sf_autotune", "sf_tuning_count", "sf_get_tuning", "sf_set_tuning"]
 
 
 class SegFockUnavailable(ImportError):
@@ -51,6 +55,14 @@ class SliceInfo(C.Structure):
     _fields_ = [("cls", C.c_int32), ("precision", C.c_int32), ("la", C.c_int32), ("lb", C.c_int32),
                 ("lc", C.c_int32), ("ld", C.c_int32), ("quartets", C.c_int64), ("prim_quartets", C.c_int64),
                 ("flop_alg", C.c_double), ("ms", C.c_float), ("threads_per_quartet", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("cls", C.c_int32), ("precision", C.c_int32), ("cost", C.c_int64), ("split", C.c_int32),
+                ("ms_default", C.c_float), ("ms_tuned", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -95,6 +107,17 @@ def lib():
     L.sf_grad_jk.argtypes = [p, p, p, i32, d, d, p]
     L.sf_grad_one_electron.argtypes = [p, p, p, i32, p, p, p, p]
     L.sf_small_solve.argtypes = [i32, p, p, p, p, p]
+    L.sf_eri_plan_create.argtypes = [p, p, i64, C.POINTER(p)]
+    L.sf_eri_plan_info.argtypes = [p, p, p, p]
+    L.sf_eri_plan_offsets.argtypes = [p, p]
+    L.sf_eri_plan_run.argtypes = [p, i32, p, p]
+    L.sf_eri_plan_destroy.argtypes = [p]
+    L.sf_eri_plan_destroy.restype = None
+    L.sf_autotune.argtypes = [p, p, i32, d, d, i32, p]
+    L.sf_tuning_count.argtypes = [p]
+    L.sf_tuning_count.restype = i32
+    L.sf_get_tuning.argtypes = [p, i32, p]
+    L.sf_set_tuning.argtypes = [p, p, i32]
     _lib = L
     return L
 

@@ -72,9 +72,17 @@ struct DBuf {
 
 struct HostTables {
   std::vector<double> t64;
-  std::vector<float> t32;
+  std::vector<float> t32, t32v;   // t32v: the FP32 kernels' layout (sf_internal.h)
+  std::vector<float4> tdd;         // the FP64 table as dd rows (sf_internal.h)
   RysAsym asym;
+  RysAsym32 asym32;
 };
+
+// split of a double into the float pair hi + lo (round to nearest twice)
+inline void dd_split(double d, float &hi, float &lo) {
+  hi = (float)d;
+  lo = (float)(d - (double)hi);
+}
 
 const HostTables &host_tables() {
   static HostTables T;
@@ -84,6 +92,36 @@ const HostTables &host_tables() {
     T.t32.assign(rys_tab_size(kTabDeg32), 0.0f);
     std::memset(&T.asym, 0, sizeof(T.asym));
     rys_build_tables(T.t64.data(), T.t32.data(), &T.asym);
+    constexpr int D = kTabDeg32;
+    T.t32v.assign(rys_tab32v_size(), 0.0f);
+    for (int n = 1; n <= kMaxRoots; ++n)
+      for (int j = 0; j < kTabNint; ++j)
+        for (int r = 0; r < n; ++r) {
+          float *row = T.t32v.data() + rys_tab32v_offset(n) + (j * n + r) * kTab32Row;
+          const float *src = T.t32.data() + rys_tab_offset(n, D) + j * (D + 1) * 2 * n;
+          for (int k = D; k >= 0; --k) {
+            row[2 * (D - k)] = src[k * 2 * n + r];
+            row[2 * (D - k) + 1] = src[k * 2 * n + n + r];
+          }
+        }
+    for (int n = 0; n <= kMaxRoots; ++n)
+      for (int i = 0; i < kMaxRoots; ++i) {
+        T.asym32.r[n][i] = (float)T.asym.r[n][i];
+        T.asym32.w[n][i] = (float)T.asym.w[n][i];
+      }
+    constexpr int D64 = kTabDeg64;
+    T.tdd.assign(rys_tabdd_size(), make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int n = 1; n <= kMaxRoots; ++n)
+      for (int j = 0; j < kTabNint; ++j)
+        for (int r = 0; r < n; ++r) {
+          float4 *row = T.tdd.data() + rys_tabdd_offset(n) + (j * n + r) * (D64 + 1);
+          const double *src = T.t64.data() + rys_tab_offset(n, D64) + j * (D64 + 1) * 2 * n;
+          for (int k = D64; k >= 0; --k) {
+            float4 &c = row[D64 - k];
+            dd_split(src[k * 2 * n + r], c.x, c.y);
+            dd_split(src[k * 2 * n + n + r], c.z, c.w);
+          }
+        }
   });
   return T;
 }
@@ -117,10 +155,21 @@ __global__ void to_float_kernel(const double *D, float *Df, int64_t n) {
   if (idx < n) Df[idx] = (float)D[idx];
 }
 
+// D as float pairs (hi, lo) for the dd kernels
+__global__ void to_dd_kernel(const double *D, float2 *Dd, int64_t n) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < n) {
+    const double d = D[idx];
+    const float hi = __double2float_rn(d);
+    Dd[idx] = make_float2(hi, __double2float_rn(d - (double)hi));
+  }
+}
+
 }  // namespace
 
 struct sf_handle {
   int device = 0;
+  int nsm = 0;                     // multiprocessors of the device
   int nshell = 0, nao = 0, natom = 0;
   std::vector<int> l, nprim, atom, ao, spoff;
   std::vector<double> cx, cy, cz, exps, coefs;
@@ -134,6 +183,10 @@ struct sf_handle {
   DBuf<double> d_pq;
   DBuf<double> d_pp64;
   DBuf<float> d_pp32;
+  DBuf<float> d_ppdd;              // records as (hi, lo) float pairs
+  DBuf<float> d_cdd;               // centres x, y, z as dd: 3 blocks of nshell (hi, lo)
+  DBuf<float4> d_tabdd;
+  DBuf<float> d_Ddd;               // density as dd (per build)
   DBuf<float> d_cx32, d_cy32, d_cz32;
   DBuf<double> d_tab64;
   DBuf<float> d_tab32;
@@ -147,7 +200,10 @@ struct sf_handle {
     ClassWork w;
     int64_t quartets, prims;
     double flops;
+    int64_t cost_hi;               // primitive cost of the segment's first quartet (tuning key)
   };
+  // autotuned primitive splits S = P*W, keyed by (class, precision, cost_hi)
+  std::vector<sf_tune_entry> tune;
   int profiling = 0;              // 1: per-slice events; 2: also serialise launches
   std::vector<cudaEvent_t> ev;   // 2 per slice while profiling
   // side streams: the class launches of one build are independent (they only
@@ -179,6 +235,20 @@ void fill_kparams(sf_handle *h) {
   k.tab64 = h->d_tab64.p;
   k.tab32 = h->d_tab32.p;
   k.asym = host_tables().asym;
+  k.asym32 = host_tables().asym32;
+  k.pdd = DevPrims<dd>{reinterpret_cast<const dd *>(h->d_ppdd.p)};
+  k.cxd = reinterpret_cast<const dd *>(h->d_cdd.p);
+  k.cyd = k.cxd + h->nshell;
+  k.czd = k.cyd + h->nshell;
+  k.tabdd = h->d_tabdd.p;
+  for (int n = 0; n <= kMaxRoots; ++n)
+    for (int i = 0; i < kMaxRoots; ++i) {
+      float a, b;
+      dd_split(host_tables().asym.r[n][i], a, b);
+      k.asymdd_r[n][i] = dd(a, b);
+      dd_split(host_tables().asym.w[n][i], a, b);
+      k.asymdd_w[n][i] = dd(a, b);
+    }
   k.nao = h->nao;
   k.natom = h->natom;
   k.err = h->d_err.p;
@@ -202,6 +272,21 @@ int64_t count_pass(const double *qy, int ny, double qi, double cut) {
   return e - qy;
 }
 
+// greedy longest-processing-time assignment of jobs (cost descending) to
+// the side streams
+std::vector<int> lpt_streams(const std::vector<double> &cost_desc) {
+  double load[sf_handle::kSideStreams] = {0};
+  std::vector<int> s(cost_desc.size(), 0);
+  for (size_t k = 0; k < cost_desc.size(); ++k) {
+    int best = 0;
+    for (int j = 1; j < sf_handle::kSideStreams; ++j)
+      if (load[j] < load[best]) best = j;
+    s[k] = best;
+    load[best] += cost_desc[k];
+  }
+  return s;
+}
+
 // Quartet lists of every (class, precision) launch for the given cutoffs.
 // Each list holds the surviving canonical quartets (bra i, ket j) of one
 // class, ordered by decreasing primitive cost K_ab K_cd (then K_ab), stable,
@@ -221,7 +306,8 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     int64_t n, prims;
     double flops;
     int x0, y0, same;
-    int psplit;
+    int psplit, wsplit;
+    int64_t cost_hi;
   };
   std::vector<Pending> pend;
   h->st_q[0] = h->st_q[1] = h->st_pq[0] = h->st_pq[1] = 0;
@@ -243,7 +329,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       int64_t mi = count_pass(qy, nY, qx[i], cut);
       if (same) mi = std::min<int64_t>(mi, i + 1);
       int64_t m6;
-      if (prec == SF_PREC_FP64) m6 = mi;
+      if (prec == SF_PREC_FP64 || prec == SF_PREC_DF) m6 = mi;
       else if (prec == SF_PREC_FP32) m6 = 0;
       else m6 = std::min<int64_t>(mi, count_pass(qy, nY, qx[i], std::max(cut32, cut)));
       m[i] = mi;
@@ -251,7 +337,10 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     }
     const int nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
     const double nabcd = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
+    // launch kind of tier pr: 0 FP64, 1 FP32, 2 double-float
+    const int hi_kind = (prec == SF_PREC_MIXED_DF || prec == SF_PREC_DF) ? 2 : 0;
     for (int pr = 0; pr < 2; ++pr) {
+      const int kind = pr == 0 ? hi_kind : 1;
       // counting sort on (K_ab, K_cd)
       std::fill(hist.begin(), hist.end(), 0);
       int64_t n = 0;
@@ -283,9 +372,11 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
         for (int64_t j = lo; j < hi; ++j) lst[pos[(size_t)ka * KB + h->pnp[y0 + j]]++] = make_int2(i, (int)j);
       }
       Pending p;
+      p.cost_hi = 0;
       p.psplit = 1;
+      p.wsplit = 1;
       p.cls = cls;
-      p.prec = pr;
+      p.prec = kind;
       p.off = all.size();
       p.x0 = x0;
       p.y0 = y0;
@@ -311,22 +402,41 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
         if (pmax > 8 && cost >= 32) return 8;
         return 1;
       };
+      // a list with fewer lanes than 8 resident warps per SM sub-partition
+      // leaves most of the GPU idle and runs at the latency of one warp's
+      // instruction stream (an FP64 instruction of one warp occupies its
+      // sub-partition's FP64 unit for 64 cycles): its quartets' primitive
+      // loops are split further, up to S_fill = P*W sub-groups per quartet,
+      // each sub-group keeping at least one primitive quartet
+      const int64_t fill = (int64_t)std::max(h->nsm, 1) * 4 * 8 * 32;
+      int sfill = 1;
+      while (p.n * T * sfill < fill && sfill < pmax * kMaxWsplit) sfill *= 2;
+      auto split_of = [&](int64_t cost) {
+        int sc = 1;
+        while (2 * sc <= cost && 2 * sc <= sfill) sc *= 2;
+        return std::max(psplit(cost), sc);
+      };
       int64_t q0 = 0;
       while (q0 < p.n) {
         const auto cost_of = [&](int64_t q) {
           return (int64_t)h->pnp[x0 + lst[q].x] * h->pnp[y0 + lst[q].y];
         };
-        const int P = psplit(cost_of(q0));
+        const int S = split_of(cost_of(q0));
         int64_t q1 = q0 + 1;
-        while (q1 < p.n && psplit(cost_of(q1)) == P) ++q1;
+        while (q1 < p.n && split_of(cost_of(q1)) == S) ++q1;
         Pending seg = p;
         seg.off = all.size() + q0;
         seg.n = q1 - q0;
+        seg.cost_hi = cost_of(q0);
+        int St = S;
+        for (const sf_tune_entry &e : h->tune)
+          if (e.cls == cls && e.precision == kind && e.cost == seg.cost_hi) St = e.split;
+        seg.psplit = std::min(St, pmax);
+        seg.wsplit = std::max(1, std::min(St / seg.psplit, kMaxWsplit));
         int64_t sp = 0;
         for (int64_t q = q0; q < q1; ++q) sp += cost_of(q);
         seg.prims = sp;
         seg.flops = (double)sp * nr * 4.0 * nabcd + 12.0 * nabcd * (double)seg.n;
-        seg.psplit = P;
         pend.push_back(seg);
         q0 = q1;
       }
@@ -342,7 +452,8 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     w.y0 = p.y0;
     w.same = p.same;
     w.psplit = p.psplit;
-    h->slices.push_back({p.cls, p.prec, w, p.n, p.prims, p.flops});
+    w.wsplit = p.wsplit;
+    h->slices.push_back({p.cls, p.prec, w, p.n, p.prims, p.flops, p.cost_hi});
   }
   // greedy longest-processing-time assignment of slices to side streams;
   // cost estimate: primitive quartets x roots x Cartesian outputs, FP64 work
@@ -355,7 +466,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       const ClassInfo &ci = kClassInfo[sl.cls];
       const double nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
       const double nc = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
-      cost[k] = (double)sl.prims * (nr * (nc + 30.0) + 40.0) * (sl.prec == 0 ? 16.0 : 1.0);
+      cost[k] = (double)sl.prims * (nr * (nc + 30.0) + 40.0) * (sl.prec == 0 ? 16.0 : sl.prec == 2 ? 5.0 : 1.0);
     }
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
@@ -363,15 +474,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     for (int k : order) sorted.push_back(h->slices[k]);
     h->slices.swap(sorted);
     std::sort(cost.begin(), cost.end(), std::greater<double>());
-    double load[sf_handle::kSideStreams] = {0};
-    h->slice_stream.assign(h->slices.size(), 0);
-    for (size_t k = 0; k < h->slices.size(); ++k) {
-      int best = 0;
-      for (int j = 1; j < sf_handle::kSideStreams; ++j)
-        if (load[j] < load[best]) best = j;
-      h->slice_stream[k] = best;
-      load[best] += cost[k];
-    }
+    h->slice_stream = lpt_streams(cost);
   }
   h->c_prec = prec;
   h->c_cut = cut;
@@ -384,19 +487,33 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
 // Run fn(k, stream) for every slice k on its side stream (forked from st,
 // joined back into st).
 template <typename F>
-int fan_out(sf_handle *h, cudaStream_t st, F &&fn) {
+int fan_out_list(sf_handle *h, cudaStream_t st, const std::vector<int> &stream_of, F &&fn) {
   SF_CK(cudaEventRecord(h->fork_ev, st));
   bool used[sf_handle::kSideStreams] = {false};
-  for (size_t k = 0; k < h->slices.size(); ++k) used[h->slice_stream[k]] = true;
+  for (int j : stream_of) used[j] = true;
   for (int j = 0; j < sf_handle::kSideStreams; ++j)
     if (used[j]) SF_CK(cudaStreamWaitEvent(h->side[j], h->fork_ev, 0));
-  for (size_t k = 0; k < h->slices.size(); ++k) SF_CK(fn(k, h->side[h->slice_stream[k]]));
+  for (size_t k = 0; k < stream_of.size(); ++k) SF_CK(fn(k, h->side[stream_of[k]]));
   for (int j = 0; j < sf_handle::kSideStreams; ++j)
     if (used[j]) {
       SF_CK(cudaEventRecord(h->join_ev[j], h->side[j]));
       SF_CK(cudaStreamWaitEvent(st, h->join_ev[j], 0));
     }
   return SF_OK;
+}
+
+template <typename F>
+int fan_out(sf_handle *h, cudaStream_t st, F &&fn) {
+  return fan_out_list(h, st, h->slice_stream, fn);
+}
+
+
+// one launch of the current quartet lists, in its kind's arithmetic
+cudaError_t launch_slice(sf_handle *h, const sf_handle::Slice &s, const ClassWork &w, const double *D,
+                         const float *D32, double *Jh, double *Kh, cudaStream_t st) {
+  if (s.prec == 0) return launch_jk_f64(s.cls, h->kp, w, D, Jh, Kh, st);
+  if (s.prec == 1) return launch_jk_f32(s.cls, h->kp, w, D32, Jh, Kh, st);
+  return launch_jk_dd(s.cls, h->kp, w, reinterpret_cast<const dd *>(h->d_Ddd.p), Jh, Kh, st);
 }
 
 // Launch every slice of the current quartet lists on the side streams
@@ -408,8 +525,7 @@ int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, d
     for (size_t k = 0; k < h->slices.size(); ++k) {
       const auto &s = h->slices[k];
       SF_CK(cudaEventRecord(h->ev[2 * k], st));
-      if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, Jh, Kh, st));
-      else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, D32, Jh, Kh, st));
+      SF_CK(launch_slice(h, s, s.w, D, D32, Jh, Kh, st));
       SF_CK(cudaEventRecord(h->ev[2 * k + 1], st));
       if (launches) ++*launches;
     }
@@ -424,8 +540,7 @@ int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, d
     const auto &s = h->slices[k];
     cudaStream_t ss = h->side[h->slice_stream[k]];
     if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k], ss));
-    if (s.prec == 0) SF_CK(launch_jk_f64(s.cls, h->kp, s.w, D, Jh, Kh, ss));
-    else SF_CK(launch_jk_f32(s.cls, h->kp, s.w, D32, Jh, Kh, ss));
+    SF_CK(launch_slice(h, s, s.w, D, D32, Jh, Kh, ss));
     if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k + 1], ss));
     if (launches) ++*launches;
   }
@@ -435,6 +550,177 @@ int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, d
       SF_CK(cudaStreamWaitEvent(st, h->join_ev[j], 0));
     }
   return SF_OK;
+}
+
+// FP32 / double-float copies of D needed by the current launch list
+int convert_density(sf_handle *h, const double *D, float *D32, cudaStream_t st, int *launches) {
+  const size_t nn = (size_t)h->nao * h->nao;
+  bool need32 = false, needdd = false;
+  for (const auto &s : h->slices) {
+    need32 |= s.prec == 1;
+    needdd |= s.prec == 2;
+  }
+  if (need32) {
+    to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, D32, (int64_t)nn);
+    SF_CK(cudaGetLastError());
+    if (launches) ++*launches;
+  }
+  if (needdd) {
+    to_dd_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, reinterpret_cast<float2 *>(h->d_Ddd.p),
+                                                                (int64_t)nn);
+    SF_CK(cudaGetLastError());
+    if (launches) ++*launches;
+  }
+  return SF_OK;
+}
+
+}  // namespace
+
+// A raw-ERI batch prepared once and run any number of times: the quartets,
+// canonicalised (l_a >= l_b, l_c >= l_d, pair class of ab >= cd) and grouped
+// by class, each class list ordered by primitive cost K_ab K_cd descending so
+// that the lanes of a warp run equal primitive loops; cut into launches by
+// the primitive split P of each precision; launches spread over the side
+// streams.  Outputs stay in input order (offsets as given, or packed).
+struct sf_eri_plan {
+  sf_handle *h = nullptr;
+  int64_t nq = 0, total = 0, prims = 0;
+  double flops = 0.0;
+  std::vector<int64_t> offsets;
+  struct Seg {
+    int cls, psplit;
+    int64_t n;
+    size_t off;
+  };
+  std::vector<Seg> segs[2];          // [FP64 and double-float (same lanes per quartet), FP32]
+  std::vector<int> seg_stream[2];
+  DBuf<int> d_pab, d_pcd, d_fl, d_str;
+  DBuf<int64_t> d_off;
+};
+
+namespace {
+
+int build_eri_plan(sf_handle *h, const int32_t *hq, int64_t nq, const int64_t *hoff, sf_eri_plan *pl) {
+  pl->h = h;
+  pl->nq = nq;
+  pl->offsets.assign(nq, 0);
+  struct Item {
+    int pab, pcd;
+    int64_t off;
+    int str[4];
+    int cost;
+  };
+  std::vector<std::vector<Item>> byc(kNumClass);
+  int64_t run = 0, maxend = 0;
+  for (int64_t q = 0; q < nq; ++q) {
+    int s[4], pos[4] = {0, 1, 2, 3};
+    for (int k = 0; k < 4; ++k) {
+      s[k] = hq[4 * q + k];
+      if (s[k] < 0 || s[k] >= h->nshell) return fail(SF_EINVAL, "sf_eri_plan: shell index out of range");
+    }
+    int nc[4], so[4];
+    for (int k = 0; k < 4; ++k) nc[k] = ncart(h->l[s[k]]);
+    so[3] = 1;
+    so[2] = nc[3];
+    so[1] = nc[2] * nc[3];
+    so[0] = nc[1] * nc[2] * nc[3];
+    const int64_t size = (int64_t)nc[0] * so[0];
+    const int64_t off = hoff ? hoff[q] : run;
+    if (off < 0) return fail(SF_EINVAL, "sf_eri_plan: negative output offset");
+    pl->offsets[q] = off;
+    run += size;
+    maxend = std::max(maxend, off + size);
+    auto before = [&](int x, int y) { return h->l[x] < h->l[y] || (h->l[x] == h->l[y] && x < y); };
+    if (before(s[0], s[1])) { std::swap(s[0], s[1]); std::swap(pos[0], pos[1]); }
+    if (before(s[2], s[3])) { std::swap(s[2], s[3]); std::swap(pos[2], pos[3]); }
+    const int X = pair_class_of(h->l[s[0]], h->l[s[1]]), Y = pair_class_of(h->l[s[2]], h->l[s[3]]);
+    int x = X, y = Y;
+    if (X < Y) {
+      std::swap(s[0], s[2]); std::swap(s[1], s[3]);
+      std::swap(pos[0], pos[2]); std::swap(pos[1], pos[3]);
+      std::swap(x, y);
+    }
+    Item it;
+    it.pab = h->pairmap[(size_t)s[0] * h->nshell + s[1]];
+    it.pcd = h->pairmap[(size_t)s[2] * h->nshell + s[3]];
+    if (it.pab < 0 || it.pcd < 0) return fail(SF_EINVAL, "sf_eri_plan: internal pair lookup failed");
+    it.off = off;
+    for (int k = 0; k < 4; ++k) it.str[k] = so[pos[k]];
+    it.cost = h->pnp[it.pab] * h->pnp[it.pcd];
+    byc[x * (x + 1) / 2 + y].push_back(it);
+  }
+  pl->total = maxend;
+  std::vector<int> pab, pcd, fl, str;
+  std::vector<int64_t> off;
+  pab.reserve(nq); pcd.reserve(nq); fl.reserve(nq); off.reserve(nq); str.reserve(4 * nq);
+  std::vector<double> cost[2];
+  for (int cls = 0; cls < kNumClass; ++cls) {
+    auto &v = byc[cls];
+    if (v.empty()) continue;
+    std::stable_sort(v.begin(), v.end(), [](const Item &a, const Item &b) { return a.cost > b.cost; });
+    const size_t base = pab.size();
+    const ClassInfo &ci = kClassInfo[cls];
+    const int nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
+    const double nabcd = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
+    for (const Item &it : v) {
+      pab.push_back(it.pab); pcd.push_back(it.pcd); fl.push_back(0); off.push_back(it.off);
+      for (int k = 0; k < 4; ++k) str.push_back(it.str[k]);
+      pl->prims += it.cost;
+      pl->flops += (double)it.cost * nr * 4.0 * nabcd;
+    }
+    for (int pr = 0; pr < 2; ++pr) {
+      const int T = pr == 0 ? ci.t64 : ci.t32;
+      const int pmax = 32 / T;
+      auto psplit = [&](int64_t c) {
+        if (pmax > 1 && c >= 4 * pmax) return pmax;
+        if (pmax > 8 && c >= 32) return 8;
+        return 1;
+      };
+      size_t q0 = 0;
+      while (q0 < v.size()) {
+        const int P = psplit(v[q0].cost);
+        size_t q1 = q0 + 1;
+        double c = v[q0].cost;
+        while (q1 < v.size() && psplit(v[q1].cost) == P) c += v[q1++].cost;
+        pl->segs[pr].push_back({cls, P, (int64_t)(q1 - q0), base + q0});
+        cost[pr].push_back(c * nr * (nabcd + 30.0));
+        q0 = q1;
+      }
+    }
+  }
+  for (int pr = 0; pr < 2; ++pr) {
+    std::vector<int> order(pl->segs[pr].size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[pr][a] > cost[pr][b]; });
+    std::vector<sf_eri_plan::Seg> sorted;
+    std::vector<double> cs;
+    for (int k : order) {
+      sorted.push_back(pl->segs[pr][k]);
+      cs.push_back(cost[pr][k]);
+    }
+    pl->segs[pr].swap(sorted);
+    pl->seg_stream[pr] = lpt_streams(cs);
+  }
+  SF_CK(pl->d_pab.upload(pab));
+  SF_CK(pl->d_pcd.upload(pcd));
+  SF_CK(pl->d_fl.upload(fl));
+  SF_CK(pl->d_str.upload(str));
+  SF_CK(pl->d_off.upload(off));
+  return SF_OK;
+}
+
+int run_eri_plan(sf_eri_plan *pl, int precision, double *out, cudaStream_t st) {
+  sf_handle *h = pl->h;
+  const int pr = precision == SF_PREC_FP32 ? 1 : 0;
+  const auto &segs = pl->segs[pr];
+  if (segs.empty()) return SF_OK;
+  return fan_out_list(h, st, pl->seg_stream[pr], [&](size_t k, cudaStream_t ss) {
+    const sf_eri_plan::Seg &sg = segs[k];
+    EriWork w{pl->d_pab.p + sg.off, pl->d_pcd.p + sg.off, pl->d_fl.p + sg.off, pl->d_off.p + sg.off,
+              pl->d_str.p + 4 * sg.off, sg.n, out, sg.psplit};
+    if (precision == SF_PREC_DF) return launch_eri_dd(sg.cls, h->kp, w, ss);
+    return launch_eri(sg.cls, pr, h->kp, w, ss);
+  });
 }
 
 }  // namespace
@@ -545,6 +831,16 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
     SF_CK(h->d_pp64.upload(rec));
     std::vector<float> rec32(rec.begin(), rec.end());
     SF_CK(h->d_pp32.upload(rec32));
+    std::vector<float> recdd(2 * rec.size());
+    for (size_t i = 0; i < rec.size(); ++i) dd_split(rec[i], recdd[2 * i], recdd[2 * i + 1]);
+    SF_CK(h->d_ppdd.upload(recdd));
+    std::vector<float> cdd(6 * (size_t)nshell);
+    for (int a = 0; a < nshell; ++a) {
+      dd_split(h->cx[a], cdd[2 * a], cdd[2 * a + 1]);
+      dd_split(h->cy[a], cdd[2 * (nshell + a)], cdd[2 * (nshell + a) + 1]);
+      dd_split(h->cz[a], cdd[2 * (2 * nshell + a)], cdd[2 * (2 * nshell + a) + 1]);
+    }
+    SF_CK(h->d_cdd.upload(cdd));
     std::vector<float> c32(h->cx.begin(), h->cx.end());
     SF_CK(h->d_cx32.upload(c32));
     c32.assign(h->cy.begin(), h->cy.end());
@@ -564,7 +860,9 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   SF_CK(h->d_coefs.upload(h->coefs));
   const HostTables &T = host_tables();
   SF_CK(h->d_tab64.upload(T.t64));
-  SF_CK(h->d_tab32.upload(T.t32));
+  SF_CK(h->d_tab32.upload(T.t32v));
+  SF_CK(h->d_tabdd.upload(T.tdd));
+  SF_CK(h->d_Ddd.alloc(2 * (size_t)nao * nao));
   SF_CK(h->d_Jh.alloc((size_t)nao * nao));
   SF_CK(h->d_Kh.alloc((size_t)nao * nao));
   SF_CK(h->d_D32.alloc((size_t)nao * nao));
@@ -577,9 +875,12 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
     SF_CK(cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming));
   }
   SF_CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
+  SF_CK(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
   SF_CK(prepare_jk_f64());
   SF_CK(prepare_jk_f32());
+  SF_CK(prepare_jk_dd());
   SF_CK(prepare_eri());
+  SF_CK(prepare_eri_dd());
   SF_CK(prepare_grad_f64());
   SF_CK(prepare_grad_f32());
   *out = guard.release();
@@ -617,12 +918,12 @@ int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out) {
   const auto &s = h->slices[idx];
   const ClassInfo &ci = kClassInfo[s.cls];
   out->cls = s.cls;
-  out->precision = s.prec == 0 ? SF_PREC_FP64 : SF_PREC_FP32;
+  out->precision = s.prec;
   out->la = ci.la; out->lb = ci.lb; out->lc = ci.lc; out->ld = ci.ld;
   out->quartets = s.quartets;
   out->prim_quartets = s.prims;
   out->flop_alg = s.flops;
-  out->threads_per_quartet = (s.prec == 0 ? ci.t64 : ci.t32) * s.w.psplit;
+  out->threads_per_quartet = (s.prec == 1 ? ci.t32 : ci.t64) * s.w.psplit * s.w.wsplit;
   out->ms = -1.0f;
   if (h->profiling && h->ev.size() >= 2 * h->slices.size()) {
     SF_CK(cudaEventSynchronize(h->ev[2 * idx + 1]));
@@ -694,7 +995,7 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
                double fp32_cutoff, sf_stats *stats, void *stream) {
   if (!h) return fail(SF_EINVAL, "sf_fock_jk: NULL handle");
   if (!D || !J || !K) return fail(SF_EINVAL, "sf_fock_jk: NULL matrix");
-  if (precision < SF_PREC_FP64 || precision > SF_PREC_MIXED) return fail(SF_EINVAL, "sf_fock_jk: bad precision");
+  if (precision < SF_PREC_FP64 || precision > SF_PREC_DF) return fail(SF_EINVAL, "sf_fock_jk: bad precision");
   if (!(cutoff >= 0.0) || !(fp32_cutoff >= 0.0)) return fail(SF_EINVAL, "sf_fock_jk: bad cutoff");
   if (!h->have_schwarz) return fail(SF_ESTATE, "sf_fock_jk: call sf_schwarz first");
   DeviceGuard g(h->device);
@@ -706,13 +1007,8 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
   SF_CK(cudaMemsetAsync(h->d_Jh.p, 0, nn * sizeof(double), st));
   SF_CK(cudaMemsetAsync(h->d_Kh.p, 0, nn * sizeof(double), st));
   int launches = 0;
-  bool need32 = false;
-  for (const auto &s : h->slices) need32 |= s.prec == 1;
-  if (need32) {
-    to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, h->d_D32.p, (int64_t)nn);
-    SF_CK(cudaGetLastError());
-    ++launches;
-  }
+  rc = convert_density(h, D, h->d_D32.p, st, &launches);
+  if (rc) return rc;
   if (h->profiling && h->ev.size() < 2 * h->slices.size()) {
     while (h->ev.size() < 2 * h->slices.size()) {
       cudaEvent_t e;
@@ -740,10 +1036,113 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
   return SF_OK;
 }
 
+int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff, double fp32_cutoff, int32_t reps,
+                void *stream) {
+  if (!h) return fail(SF_EINVAL, "sf_autotune: NULL handle");
+  if (!D) return fail(SF_EINVAL, "sf_autotune: NULL density");
+  if (precision < SF_PREC_FP64 || precision > SF_PREC_DF) return fail(SF_EINVAL, "sf_autotune: bad precision");
+  if (!(cutoff >= 0.0) || !(fp32_cutoff >= 0.0)) return fail(SF_EINVAL, "sf_autotune: bad cutoff");
+  if (reps < 1 || reps > 1000) return fail(SF_EINVAL, "sf_autotune: reps must be in 1..1000");
+  if (!h->have_schwarz) return fail(SF_ESTATE, "sf_autotune: call sf_schwarz first");
+  DeviceGuard g(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = build_work(h, precision, cutoff, fp32_cutoff);
+  if (rc) return rc;
+  rc = convert_density(h, D, h->d_D32.p, st, nullptr);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  SF_CK(cudaEventCreate(&e0));
+  SF_CK(cudaEventCreate(&e1));
+  // every candidate adds into the handle's scratch Jh/Kh, which the next
+  // Fock build clears; the caller's matrices are not touched
+  auto time_split = [&](const sf_handle::Slice &sl, int S, float *ms) -> cudaError_t {
+    const ClassInfo &ci = kClassInfo[sl.cls];
+    const int pmax = 32 / (sl.prec == 1 ? ci.t32 : ci.t64);
+    ClassWork w = sl.w;
+    w.psplit = std::min(S, pmax);
+    w.wsplit = S / w.psplit;
+    auto launch = [&]() { return launch_slice(h, sl, w, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st); };
+    cudaError_t e = launch();   // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    *ms /= (float)reps;
+    return e;
+  };
+  int tuned = 0;
+  for (auto &sl : h->slices) {
+    const ClassInfo &ci = kClassInfo[sl.cls];
+    const int pmax = 32 / (sl.prec == 1 ? ci.t32 : ci.t64);
+    const int S0 = sl.w.psplit * sl.w.wsplit;
+    float ms0 = 0.f;
+    cudaError_t e = time_split(sl, S0, &ms0);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return fail(SF_ECUDA, std::string("sf_autotune: ") + cudaGetErrorString(e));
+    }
+    int best = S0;
+    float bms = ms0;
+    for (int S : {S0 / 4, S0 / 2, S0 * 2, S0 * 4}) {
+      if (S < 1 || S > pmax * kMaxWsplit || S > 2 * std::max<int64_t>(sl.cost_hi, 1)) continue;
+      float ms = 0.f;
+      e = time_split(sl, S, &ms);
+      if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return fail(SF_ECUDA, std::string("sf_autotune: ") + cudaGetErrorString(e));
+      }
+      if (ms < 0.97f * bms) {   // keep the heuristic unless a split is clearly faster
+        bms = ms;
+        best = S;
+      }
+    }
+    sl.w.psplit = std::min(best, pmax);
+    sl.w.wsplit = best / sl.w.psplit;
+    sf_tune_entry te{sl.cls, sl.prec, sl.cost_hi, best, ms0, bms};
+    bool found = false;
+    for (auto &x : h->tune)
+      if (x.cls == te.cls && x.precision == te.precision && x.cost == te.cost) {
+        x = te;
+        found = true;
+      }
+    if (!found) h->tune.push_back(te);
+    ++tuned;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return tuned;
+}
+
+int32_t sf_tuning_count(const sf_handle *h) { return h ? (int32_t)h->tune.size() : -1; }
+
+int sf_get_tuning(const sf_handle *h, int32_t idx, sf_tune_entry *out) {
+  if (!h || !out || idx < 0 || idx >= (int32_t)h->tune.size()) return fail(SF_EINVAL, "sf_get_tuning: bad arguments");
+  *out = h->tune[idx];
+  return SF_OK;
+}
+
+int sf_set_tuning(sf_handle *h, const sf_tune_entry *entries, int32_t n) {
+  if (!h || n < 0 || (n > 0 && !entries)) return fail(SF_EINVAL, "sf_set_tuning: bad arguments");
+  for (int32_t i = 0; i < n; ++i) {
+    const sf_tune_entry &e = entries[i];
+    if (e.cls < 0 || e.cls >= kNumClass || e.precision < 0 || e.precision > 2 || e.split < 1 ||
+        e.split > 32 * kMaxWsplit || (e.split & (e.split - 1)))
+      return fail(SF_EINVAL, "sf_set_tuning: bad entry " + std::to_string(i));
+  }
+  h->tune.assign(entries, entries + n);
+  h->c_prec = -1;   // rebuild the launch list with the new splits
+  return SF_OK;
+}
+
 int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int32_t precision, double cutoff,
                        double fp32_cutoff, void *stream) {
   if (!h) return fail(SF_EINVAL, "sf_fock_jk_noalloc: NULL handle");
   if (!D || !J || !K) return fail(SF_EINVAL, "sf_fock_jk_noalloc: NULL matrix");
+  if (precision == SF_PREC_MIXED_DF || precision == SF_PREC_DF)
+    return fail(SF_EUNSUPPORTED, "sf_fock_jk_noalloc: the double-float modes need the handle's scratch (sf_fock_jk)");
   if (precision < SF_PREC_FP64 || precision > SF_PREC_MIXED) return fail(SF_EINVAL, "sf_fock_jk_noalloc: bad precision");
   if (h->nao > SF_NOALLOC_MAX_NAO)
     return fail(SF_EINVAL, "sf_fock_jk_noalloc: nao = " + std::to_string(h->nao) +
@@ -790,7 +1189,11 @@ int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, d
                void *stream) {
   if (!h) return fail(SF_EINVAL, "sf_grad_jk: NULL handle");
   if (!D || !grad) return fail(SF_EINVAL, "sf_grad_jk: NULL pointer");
-  if (precision < SF_PREC_FP64 || precision > SF_PREC_MIXED) return fail(SF_EINVAL, "sf_grad_jk: bad precision");
+  if (precision < SF_PREC_FP64 || precision > SF_PREC_DF) return fail(SF_EINVAL, "sf_grad_jk: bad precision");
+  // the derivative kernels have FP64 and FP32 forms: the double-float modes
+  // take FP64 for their accurate tier
+  if (precision == SF_PREC_MIXED_DF) precision = SF_PREC_MIXED;
+  if (precision == SF_PREC_DF) precision = SF_PREC_FP64;
   if (!(cutoff >= 0.0) || !(fp32_cutoff >= 0.0)) return fail(SF_EINVAL, "sf_grad_jk: bad cutoff");
   if (!h->have_schwarz) return fail(SF_ESTATE, "sf_grad_jk: call sf_schwarz first");
   DeviceGuard g(h->device);
@@ -861,7 +1264,8 @@ int sf_eri_batch(sf_handle *h, const int32_t *quartets, int64_t nq, int32_t prec
                  const int64_t *out_offsets, void *stream) {
   if (!h) return fail(SF_EINVAL, "sf_eri_batch: NULL handle");
   if (nq < 0 || (nq > 0 && (!quartets || !out || !out_offsets))) return fail(SF_EINVAL, "sf_eri_batch: bad arguments");
-  if (precision != SF_PREC_FP64 && precision != SF_PREC_FP32) return fail(SF_EINVAL, "sf_eri_batch: bad precision");
+  if (precision != SF_PREC_FP64 && precision != SF_PREC_FP32 && precision != SF_PREC_DF)
+    return fail(SF_EINVAL, "sf_eri_batch: bad precision");
   if (nq == 0) return SF_OK;
   DeviceGuard g(h->device);
   cudaStream_t st = (cudaStream_t)stream;
@@ -870,57 +1274,56 @@ int sf_eri_batch(sf_handle *h, const int32_t *quartets, int64_t nq, int32_t prec
   SF_CK(cudaMemcpyAsync(hq.data(), quartets, hq.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   SF_CK(cudaMemcpyAsync(hoff.data(), out_offsets, hoff.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   SF_CK(cudaStreamSynchronize(st));
-  struct Item { int pab, pcd, flags; int64_t off; int str[4]; };
-  std::vector<std::vector<Item>> byc(kNumClass);
-  for (int64_t q = 0; q < nq; ++q) {
-    int s[4], pos[4] = {0, 1, 2, 3};
-    for (int k = 0; k < 4; ++k) {
-      s[k] = hq[4 * q + k];
-      if (s[k] < 0 || s[k] >= h->nshell) return fail(SF_EINVAL, "sf_eri_batch: shell index out of range");
-    }
-    int nc[4], so[4];
-    for (int k = 0; k < 4; ++k) nc[k] = ncart(h->l[s[k]]);
-    so[3] = 1;
-    so[2] = nc[3];
-    so[1] = nc[2] * nc[3];
-    so[0] = nc[1] * nc[2] * nc[3];
-    auto before = [&](int x, int y) { return h->l[x] < h->l[y] || (h->l[x] == h->l[y] && x < y); };
-    if (before(s[0], s[1])) { std::swap(s[0], s[1]); std::swap(pos[0], pos[1]); }
-    if (before(s[2], s[3])) { std::swap(s[2], s[3]); std::swap(pos[2], pos[3]); }
-    const int X = pair_class_of(h->l[s[0]], h->l[s[1]]), Y = pair_class_of(h->l[s[2]], h->l[s[3]]);
-    int x = X, y = Y;
-    if (X < Y) {
-      std::swap(s[0], s[2]); std::swap(s[1], s[3]);
-      std::swap(pos[0], pos[2]); std::swap(pos[1], pos[3]);
-      std::swap(x, y);
-    }
-    Item it;
-    it.pab = h->pairmap[(size_t)s[0] * h->nshell + s[1]];
-    it.pcd = h->pairmap[(size_t)s[2] * h->nshell + s[3]];
-    if (it.pab < 0 || it.pcd < 0) return fail(SF_EINVAL, "sf_eri_batch: internal pair lookup failed");
-    it.flags = 0;
-    it.off = hoff[q];
-    for (int k = 0; k < 4; ++k) it.str[k] = so[pos[k]];
-    byc[x * (x + 1) / 2 + y].push_back(it);
-  }
-  for (int cls = 0; cls < kNumClass; ++cls) {
-    const auto &v = byc[cls];
-    if (v.empty()) continue;
-    std::vector<int> pab(v.size()), pcd(v.size()), fl(v.size()), str(4 * v.size());
-    std::vector<int64_t> off(v.size());
-    for (size_t i = 0; i < v.size(); ++i) {
-      pab[i] = v[i].pab; pcd[i] = v[i].pcd; fl[i] = v[i].flags; off[i] = v[i].off;
-      for (int k = 0; k < 4; ++k) str[4 * i + k] = v[i].str[k];
-    }
-    DBuf<int> dpab, dpcd, dfl, dstr;
-    DBuf<int64_t> doff;
-    SF_CK(dpab.upload(pab)); SF_CK(dpcd.upload(pcd)); SF_CK(dfl.upload(fl)); SF_CK(dstr.upload(str));
-    SF_CK(doff.upload(off));
-    EriWork w{dpab.p, dpcd.p, dfl.p, doff.p, dstr.p, (int64_t)v.size(), out};
-    SF_CK(launch_eri(cls, precision == SF_PREC_FP32, h->kp, w, st));
-    SF_CK(cudaStreamSynchronize(st));
-  }
+  sf_eri_plan pl;
+  int rc = build_eri_plan(h, hq.data(), nq, hoff.data(), &pl);
+  if (rc) return rc;
+  rc = run_eri_plan(&pl, precision, out, st);
+  if (rc) return rc;
+  SF_CK(cudaStreamSynchronize(st));   // the plan's device lists are freed on return
   return SF_OK;
+}
+
+int sf_eri_plan_create(sf_handle *h, const int32_t *quartets, int64_t nq, sf_eri_plan **out) {
+  if (!out) return fail(SF_EINVAL, "sf_eri_plan_create: out is NULL");
+  *out = nullptr;
+  if (!h) return fail(SF_EINVAL, "sf_eri_plan_create: NULL handle");
+  if (nq < 0 || (nq > 0 && !quartets)) return fail(SF_EINVAL, "sf_eri_plan_create: bad arguments");
+  DeviceGuard g(h->device);
+  std::unique_ptr<sf_eri_plan> pl(new sf_eri_plan);
+  int rc = build_eri_plan(h, quartets, nq, nullptr, pl.get());
+  if (rc) return rc;
+  *out = pl.release();
+  return SF_OK;
+}
+
+int sf_eri_plan_info(const sf_eri_plan *pl, int64_t *outputs, int64_t *prim_quartets, double *flop_alg) {
+  if (!pl) return fail(SF_EINVAL, "sf_eri_plan_info: NULL plan");
+  if (outputs) *outputs = pl->total;
+  if (prim_quartets) *prim_quartets = pl->prims;
+  if (flop_alg) *flop_alg = pl->flops;
+  return SF_OK;
+}
+
+int sf_eri_plan_offsets(const sf_eri_plan *pl, int64_t *offsets) {
+  if (!pl || (pl->nq > 0 && !offsets)) return fail(SF_EINVAL, "sf_eri_plan_offsets: bad arguments");
+  if (pl->nq > 0) std::memcpy(offsets, pl->offsets.data(), (size_t)pl->nq * sizeof(int64_t));
+  return SF_OK;
+}
+
+int sf_eri_plan_run(sf_eri_plan *pl, int32_t precision, double *out, void *stream) {
+  if (!pl) return fail(SF_EINVAL, "sf_eri_plan_run: NULL plan");
+  if (precision != SF_PREC_FP64 && precision != SF_PREC_FP32 && precision != SF_PREC_DF)
+    return fail(SF_EINVAL, "sf_eri_plan_run: bad precision");
+  if (pl->nq > 0 && !out) return fail(SF_EINVAL, "sf_eri_plan_run: NULL output");
+  DeviceGuard g(pl->h->device);
+  return run_eri_plan(pl, precision, out, (cudaStream_t)stream);
+}
+
+void sf_eri_plan_destroy(sf_eri_plan *pl) {
+  if (!pl) return;
+  DeviceGuard g(pl->h->device);
+  cudaDeviceSynchronize();   // runs in flight still read the plan's lists
+  delete pl;
 }
 
 int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges, int32_t natom, double *S, double *T,

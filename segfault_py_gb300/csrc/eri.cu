@@ -7,10 +7,14 @@ namespace sf {
 template <int LA, int LB, int LC, int LD, typename R, int T>
 static cudaError_t run_eri(const KParams &kp, const EriWork &w, cudaStream_t st) {
   if (w.n <= 0) return cudaSuccess;
-  constexpr int G = kBlock / T;
+  const int P = w.psplit < 1 ? 1 : w.psplit;
+  if (T * P > 32 || (P & (P - 1))) return cudaErrorInvalidValue;
+  EriWork w2 = w;
+  w2.psplit = P;
+  const int G = kBlock / (T * P);
   constexpr size_t smem = grp_smem<LA, LB, LC, LD, R, T>();
   const int64_t grid = (w.n + G - 1) / G;
-  eri_kernel<LA, LB, LC, LD, R, T><<<(unsigned)grid, kBlock, smem, st>>>(kp, w);
+  eri_kernel<LA, LB, LC, LD, R, T><<<(unsigned)grid, kBlock, smem, st>>>(kp, w2);
   return cudaGetLastError();
 }
 

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, c
     __syncthreads();
   }
   const int TP0 = T * w.psplit;
-  const int64_t q0 = (int64_t)blockIdx.x * (kBlock / TP0) + threadIdx.x / TP0;
+  const int64_t q0 = ((int64_t)blockIdx.x * (kBlock / TP0) + threadIdx.x / TP0) / w.wsplit;
   if (q0 < w.n) grad_quartet<LA, LB, LC, LD, R, T>(kp, w, D, cta_sum ? sgrad : grad, cta_sum);
   if (cta_sum) {
     __syncthreads();
@@ -163,10 +163,13 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
   using G = QG<LA, LB, LC, LD>;
   using GP = GGrp<LA, LB, LC, LD, R, T>;
   constexpr int NR = G::NRG, SZ = G::SZE, NPER = GP::NPER;
-  const int P = w.psplit;
+  const int P = w.psplit, W = w.wsplit;
   const int TP = T * P;
-  const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
-  const int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp;
+  const int grp = threadIdx.x / TP, t = threadIdx.x % T;
+  const int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;
+  const int64_t q = gid / W;
+  const int pl = (threadIdx.x / T) % P;
+  const int sub = (int)(gid - q * W) * P + pl;   // primitive sub-group of the W*P
   const int2 ij = __ldg(w.list + q);
   const int pab = w.x0 + ij.x, pcd = w.y0 + ij.y;
   const QGeom<R> g = make_geom<R>(kp, pab, pcd, false, false);
@@ -206,13 +209,13 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
   }
   R gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
   if constexpr (T == 1) {
-    grad_t1<LA, LB, LC, LD, R>(kp, g, gam, p, P, gA, gB, gC);
+    grad_t1<LA, LB, LC, LD, R>(kp, g, gam, sub, W * P, gA, gB, gC);
   } else {
   const int nprim = g.ab_n * g.cd_n;
   int cur = -1;
   PQ<R> s;
   R pp, px, py, pz, kab, al = 0, be = 0;
-  for (int idx = p; idx < nprim; idx += P) {
+  for (int idx = sub; idx < nprim; idx += W * P) {
     const int ip = idx / g.cd_n, iq = idx - ip * g.cd_n;
     if (ip != cur) {
       load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
@@ -294,7 +297,7 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
       gB[d] += __shfl_xor_sync(qmask, gB[d], sft);
       gC[d] += __shfl_xor_sync(qmask, gC[d], sft);
     }
-  if (t == 0 && p == 0) {
+  if (t == 0 && pl == 0) {
     const int at_a = kp.sh.atom[g.a], at_b = kp.sh.atom[g.b], at_c = kp.sh.atom[g.c], at_d = kp.sh.atom[g.d];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {

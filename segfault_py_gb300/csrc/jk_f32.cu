@@ -9,12 +9,12 @@ static cudaError_t run_jk32(const KParams &kp, const ClassWork &w, const float *
                             cudaStream_t st) {
   const int64_t n = w.n;
   if (n <= 0) return cudaSuccess;
-  const int P = w.psplit < 1 ? 1 : w.psplit;
-  if (T * P > 32 || (P & (P - 1))) return cudaErrorInvalidValue;
+  const int P = w.psplit < 1 ? 1 : w.psplit, W = w.wsplit < 1 ? 1 : w.wsplit;
+  if (T * P > 32 || (P & (P - 1)) || W > kMaxWsplit) return cudaErrorInvalidValue;
   const int G = kBlock / (T * P);
   constexpr size_t smem = grp_smem<LA, LB, LC, LD, float, T>();
   auto kern = jk_kernel<LA, LB, LC, LD, float, T>;
-  const int64_t grid = (n + G - 1) / G;
+  const int64_t grid = (n * W + G - 1) / G;
   kern<<<(unsigned)grid, kBlock, smem, st>>>(kp, w, D, Jh, Kh);
   return cudaGetLastError();
 }

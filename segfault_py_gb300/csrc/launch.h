@@ -8,8 +8,11 @@ cudaError_t launch_jk_f64(int cls, const KParams &kp, const ClassWork &w, const 
                           cudaStream_t st);
 cudaError_t launch_jk_f32(int cls, const KParams &kp, const ClassWork &w, const float *D, double *Jh, double *Kh,
                           cudaStream_t st);
-// raw integrals of one class
+cudaError_t launch_jk_dd(int cls, const KParams &kp, const ClassWork &w, const dd *D, double *Jh, double *Kh,
+                         cudaStream_t st);
+// raw integrals of one class (fp32: FP32 evaluation, else FP64)
 cudaError_t launch_eri(int cls, int fp32, const KParams &kp, const EriWork &w, cudaStream_t st);
+cudaError_t launch_eri_dd(int cls, const KParams &kp, const EriWork &w, cudaStream_t st);
 // Schwarz bounds of pair class pc (0..5) over pairs [p0, p0+n)
 cudaError_t launch_schwarz(int pc, const KParams &kp, int p0, int n, double *qout, cudaStream_t st);
 
@@ -21,6 +24,8 @@ cudaError_t prepare_grad_f64();
 cudaError_t prepare_grad_f32();
 cudaError_t prepare_jk_f64();
 cudaError_t prepare_jk_f32();
+cudaError_t prepare_jk_dd();
+cudaError_t prepare_eri_dd();
 cudaError_t prepare_eri();
 
 // one-electron kernel parameters (oneint.cu)

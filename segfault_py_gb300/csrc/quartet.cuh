@@ -24,7 +24,9 @@
 // Epilogues: J/K digestion (fock), store (eri batch), diagonal max (Schwarz).
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
+#include "dd.cuh"
 #include "sf_internal.h"
 
 namespace sf {
@@ -35,8 +37,15 @@ struct KParams {
   DevPrims<double> p64;
   DevPrims<float> p32;
   const double *tab64;
-  const float *tab32;
+  const float *tab32;  // FP32 kernel layout (rys_tab32v_offset)
   RysAsym asym;
+  RysAsym32 asym32;
+  // double-float copies: primitive-pair records (8 dd), centres, the FP64
+  // Rys table as dd rows (rys_tabdd_offset) and the asymptotic constants
+  DevPrims<dd> pdd;
+  const dd *cxd, *cyd, *czd;
+  const float4 *tabdd;
+  dd asymdd_r[kMaxRoots + 1][kMaxRoots], asymdd_w[kMaxRoots + 1][kMaxRoots];
   int nao;
   int natom;           // atoms referenced by the shells (gradient length / 3)
   int *err;            // device error flag (unused by the arithmetic kernels)
@@ -48,6 +57,16 @@ template <>
 __device__ __forceinline__ const DevPrims<double> &prims_of<double>(const KParams &kp) { return kp.p64; }
 template <>
 __device__ __forceinline__ const DevPrims<float> &prims_of<float>(const KParams &kp) { return kp.p32; }
+template <>
+__device__ __forceinline__ const DevPrims<dd> &prims_of<dd>(const KParams &kp) { return kp.pdd; }
+
+// type-generic loads, shuffles and conversions
+__device__ __forceinline__ float ldg_r(const float *p) { return __ldg(p); }
+__device__ __forceinline__ double ldg_r(const double *p) { return __ldg(p); }
+__device__ __forceinline__ dd ldg_r(const dd *p) { return dd_ldg(p); }
+__device__ __forceinline__ float shfl_xor_r(unsigned m, float v, int k) { return __shfl_xor_sync(m, v, k); }
+__device__ __forceinline__ double shfl_xor_r(unsigned m, double v, int k) { return __shfl_xor_sync(m, v, k); }
+__device__ __forceinline__ dd shfl_xor_r(unsigned m, dd v, int k) { return dd_shfl_xor(m, v, k); }
 
 // 1/sqrt(a): single-precision hardware seed + two Newton-Raphson steps
 // y <- y (3/2 - a/2 y^2) (quadratic convergence: 2^-23 -> 2^-46 -> rounding).
@@ -59,6 +78,7 @@ __device__ __forceinline__ double rsqrt_nr(double a) {
   return y;
 }
 __device__ __forceinline__ float rsqrt_nr(float a) { return rsqrtf(a); }
+__device__ __forceinline__ dd rsqrt_nr(dd a) { return dd_rsqrt(a); }
 
 template <typename R>
 struct TabDeg;
@@ -82,11 +102,92 @@ struct Vec2<double> { using T = double2; };
 template <>
 struct Vec2<float> { using T = float2; };
 
-// all n roots (u = t^2) and weights at x.  Coefficient row k of an interval
-// holds the 2N values (u_0..u_{N-1}, w_0..w_{N-1}); rows are loaded as N
-// two-value vectors (the table offsets are all even).
+// FP32: root r at x from its row of (u_k, w_k) pairs, Horner in the row's
+// order k = D .. 0
+__device__ __forceinline__ void rys_row_f32(const float *row, float s, float &u, float &w) {
+  const float2 *c = reinterpret_cast<const float2 *>(row);
+  const float2 top = __ldg(c);
+  u = top.x;
+  w = top.y;
+#pragma unroll
+  for (int k = 1; k <= kTabDeg32; ++k) {
+    const float2 v = __ldg(c + k);
+    u = u * s + v.x;
+    w = w * s + v.y;
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void rys_roots_all_f32(const KParams &kp, float x, float (&u)[N], float (&w)[N]) {
+  if (x >= (float)kTabXmax) {
+    const float ix = 1.0f / x, isx = rsqrtf(x);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      u[i] = kp.asym32.r[N][i] * ix;
+      w[i] = kp.asym32.w[N][i] * isx;
+    }
+    return;
+  }
+  const int j = (int)x;
+  const float s = 2.0f * (x - (float)j) - 1.0f;
+  const float *base = kp.tab32 + rys_tab32v_offset(N) + j * N * kTab32Row;
+#pragma unroll
+  for (int i = 0; i < N; ++i) rys_row_f32(base + i * kTab32Row, s, u[i], w[i]);
+}
+
+// dd: the FP64 table's coefficients as dd rows: per n-root block, interval
+// j, root r, the (D+1) coefficients from k = D down to 0, each one 16-byte
+// (u_hi, u_lo, w_hi, w_lo); Horner in dd
+__device__ __forceinline__ void rys_row_dd(const float4 *row, dd s, dd &u, dd &w) {
+  const float4 top = __ldg(row);
+  u = dd(top.x, top.y);
+  w = dd(top.z, top.w);
+#pragma unroll
+  for (int k = 1; k <= kTabDeg64; ++k) {
+    const float4 c = __ldg(row + k);
+    u = dd_fma(u, s, dd(c.x, c.y));
+    w = dd_fma(w, s, dd(c.z, c.w));
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void rys_roots_all_dd(const KParams &kp, dd x, dd (&u)[N], dd (&w)[N]) {
+  if (x.hi >= (float)kTabXmax) {
+    const dd ix = dd_recip(x), isx = dd_rsqrt(x);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      u[i] = kp.asymdd_r[N][i] * ix;
+      w[i] = kp.asymdd_w[N][i] * isx;
+    }
+    return;
+  }
+  const int j = (int)x.hi;
+  const dd s = (x - dd((float)j)) * 2.0f - dd(1.0f);
+  const float4 *base = kp.tabdd + rys_tabdd_offset(N) + j * N * (kTabDeg64 + 1);
+#pragma unroll
+  for (int i = 0; i < N; ++i) rys_row_dd(base + i * (kTabDeg64 + 1), s, u[i], w[i]);
+}
+
+// all n roots (u = t^2) and weights at x.  FP64: coefficient row k of an
+// interval holds the 2N values (u_0..u_{N-1}, w_0..w_{N-1}); rows are loaded
+// as N two-value vectors (the table offsets are all even).
+template <int N>
+__device__ __forceinline__ void rys_roots_all_f64(const KParams &kp, double x, double (&u)[N], double (&w)[N]);
+
 template <int N, typename R>
 __device__ __forceinline__ void rys_roots_all(const KParams &kp, R x, R (&u)[N], R (&w)[N]) {
+  if constexpr (std::is_same<R, float>::value) {
+    rys_roots_all_f32<N>(kp, x, u, w);
+  } else if constexpr (std::is_same<R, dd>::value) {
+    rys_roots_all_dd<N>(kp, x, u, w);
+  } else {
+    rys_roots_all_f64<N>(kp, x, u, w);
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void rys_roots_all_f64(const KParams &kp, double x, double (&u)[N], double (&w)[N]) {
+  using R = double;
   if (x >= (R)kTabXmax) {
     const R ix = (R)1 / x, isx = rsqrt_nr(x);
 #pragma unroll
@@ -125,8 +226,37 @@ __device__ __forceinline__ void rys_roots_all(const KParams &kp, R x, R (&u)[N],
 }
 
 // one root r of the n-point rule
+template <int N>
+__device__ __forceinline__ void rys_root_one_f64(const KParams &kp, double x, int r, double &u, double &w);
+
 template <int N, typename R>
 __device__ __forceinline__ void rys_root_one(const KParams &kp, R x, int r, R &u, R &w) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (x >= (float)kTabXmax) {
+      u = kp.asym32.r[N][r] / x;
+      w = kp.asym32.w[N][r] * rsqrtf(x);
+      return;
+    }
+    const int j = (int)x;
+    const float s = 2.0f * (x - (float)j) - 1.0f;
+    rys_row_f32(kp.tab32 + rys_tab32v_offset(N) + (j * N + r) * kTab32Row, s, u, w);
+  } else if constexpr (std::is_same<R, dd>::value) {
+    if (x.hi >= (float)kTabXmax) {
+      u = kp.asymdd_r[N][r] * dd_recip(x);
+      w = kp.asymdd_w[N][r] * dd_rsqrt(x);
+      return;
+    }
+    const int j = (int)x.hi;
+    const dd s = (x - dd((float)j)) * 2.0f - dd(1.0f);
+    rys_row_dd(kp.tabdd + rys_tabdd_offset(N) + (j * N + r) * (kTabDeg64 + 1), s, u, w);
+  } else {
+    rys_root_one_f64<N>(kp, x, r, u, w);
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void rys_root_one_f64(const KParams &kp, double x, int r, double &u, double &w) {
+  using R = double;
   if (x >= (R)kTabXmax) {
     u = (R)kp.asym.r[N][r] / x;
     w = (R)kp.asym.w[N][r] * rsqrt_nr(x);
@@ -245,6 +375,11 @@ template <>
 __device__ __forceinline__ const float *centre_of<float>(const DevShells &sh, int d) {
   return d == 0 ? sh.cx32 : d == 1 ? sh.cy32 : sh.cz32;
 }
+template <typename R>
+__device__ __forceinline__ const R *centre_in(const KParams &kp, int d) {
+  if constexpr (std::is_same<R, dd>::value) return d == 0 ? kp.cxd : d == 1 ? kp.cyd : kp.czd;
+  else return centre_of<R>(kp.sh, d);
+}
 
 // geometry in the working precision R (the FP32 kernels read single-precision
 // centres and never touch the FP64 pipe here)
@@ -257,7 +392,7 @@ __device__ __forceinline__ QGeom<R> make_geom(const KParams &kp, int pab, int pc
   g.a = a; g.b = b; g.c = c; g.d = d;
   g.ab_off = kp.pr.poff[pab]; g.ab_n = kp.pr.np[pab];
   g.cd_off = kp.pr.poff[pcd]; g.cd_n = kp.pr.np[pcd];
-  const R *X = centre_of<R>(kp.sh, 0), *Y = centre_of<R>(kp.sh, 1), *Z = centre_of<R>(kp.sh, 2);
+  const R *X = centre_in<R>(kp, 0), *Y = centre_in<R>(kp, 1), *Z = centre_in<R>(kp, 2);
   g.Ax = X[a]; g.Ay = Y[a]; g.Az = Z[a];
   g.Cx = X[c]; g.Cy = Y[c]; g.Cz = Z[c];
   g.ABx = g.Ax - X[b]; g.ABy = g.Ay - Y[b]; g.ABz = g.Az - Z[b];
@@ -289,6 +424,13 @@ __device__ __forceinline__ void load_rec<double>(const double *rec, double &p, d
   const double2 b = __ldg(reinterpret_cast<const double2 *>(rec + 2));
   const double2 c = __ldg(reinterpret_cast<const double2 *>(rec + 4));
   p = a.x; px = a.y; py = b.x; pz = b.y; k = c.x; i2p = c.y;
+}
+
+template <>
+__device__ __forceinline__ void load_rec<dd>(const dd *rec, dd &p, dd &px, dd &py, dd &pz, dd &k, dd &i2p) {
+  const float4 *r4 = reinterpret_cast<const float4 *>(rec);
+  const float4 a = __ldg(r4), b = __ldg(r4 + 1), c = __ldg(r4 + 2);
+  p = dd(a.x, a.y); px = dd(a.z, a.w); py = dd(b.x, b.y); pz = dd(b.z, b.w); k = dd(c.x, c.y); i2p = dd(c.z, c.w);
 }
 
 template <typename R>
@@ -326,6 +468,7 @@ __device__ __forceinline__ double f2d_alu(float f) {
 }
 __device__ __forceinline__ double to_f64(float f) { return f2d_alu(f); }
 __device__ __forceinline__ double to_f64(double f) { return f; }
+__device__ __forceinline__ double to_f64(dd f) { return f2d_alu(f.hi) + f2d_alu(f.lo); }
 
 // ---------------------------------------------------------------------------
 // T == 1: whole quartet in registers; acc[o] unnormalised
@@ -453,7 +596,7 @@ template <typename R, int N, int T>
 __device__ __forceinline__ void reduce_psplit(R (&acc)[N], int P, unsigned qmask) {
   for (int sft = T; sft < T * P; sft <<= 1) {
 #pragma unroll
-    for (int k = 0; k < N; ++k) acc[k] += __shfl_xor_sync(qmask, acc[k], sft);
+    for (int k = 0; k < N; ++k) acc[k] += shfl_xor_r(qmask, acc[k], sft);
   }
 }
 
@@ -483,7 +626,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
       for (int ic = 0; ic < Q::NC; ++ic)
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id)
-          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (c0 + ic) * n + d0 + id);
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * ldg_r(D + (c0 + ic) * n + d0 + id);
       atomicAdd(Jh + (a0 + ia) * n + b0 + ib, to_f64((R)2 * scale * s));
     }
 #pragma unroll
@@ -495,7 +638,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
       for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
         for (int ib = 0; ib < Q::NB; ++ib)
-          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + b0 + ib);
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * ldg_r(D + (a0 + ia) * n + b0 + ib);
       atomicAdd(Jh + (c0 + ic) * n + d0 + id, to_f64((R)2 * scale * s));
     }
 #pragma unroll
@@ -507,7 +650,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
       for (int ib = 0; ib < Q::NB; ++ib)
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id)
-          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (b0 + ib) * n + d0 + id);
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * ldg_r(D + (b0 + ib) * n + d0 + id);
       atomicAdd(Kh + (a0 + ia) * n + c0 + ic, to_f64(scale * s));
     }
 #pragma unroll
@@ -519,7 +662,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
       for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id)
-          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + d0 + id);
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * ldg_r(D + (a0 + ia) * n + d0 + id);
       atomicAdd(Kh + (b0 + ib) * n + c0 + ic, to_f64(scale * s));
     }
 #pragma unroll
@@ -531,7 +674,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
       for (int ib = 0; ib < Q::NB; ++ib)
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic)
-          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (b0 + ib) * n + c0 + ic);
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * ldg_r(D + (b0 + ib) * n + c0 + ic);
       atomicAdd(Kh + (a0 + ia) * n + d0 + id, to_f64(scale * s));
     }
 #pragma unroll
@@ -543,7 +686,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
       for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
         for (int ic = 0; ic < Q::NC; ++ic)
-          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * __ldg(D + (a0 + ia) * n + c0 + ic);
+          s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * ldg_r(D + (a0 + ia) * n + c0 + ic);
       atomicAdd(Kh + (b0 + ib) * n + d0 + id, to_f64(scale * s));
     }
 }
@@ -574,32 +717,32 @@ __device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
     if (e < E0) {
       const int ia = e / NB, ib = e % NB;
       for (int ic = 0; ic < NC; ++ic)
-        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (c0 + ic) * n + d0 + id);
+        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * ldg_r(D + (c0 + ic) * n + d0 + id);
       atomicAdd(Jh + (a0 + ia) * n + b0 + ib, to_f64((R)2 * scale * s));
     } else if (e < E1) {
       const int ic = (e - E0) / ND, id = (e - E0) % ND;
       for (int ia = 0; ia < NA; ++ia)
-        for (int ib = 0; ib < NB; ++ib) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + b0 + ib);
+        for (int ib = 0; ib < NB; ++ib) s += V4(ia, ib, ic, id) * ldg_r(D + (a0 + ia) * n + b0 + ib);
       atomicAdd(Jh + (c0 + ic) * n + d0 + id, to_f64((R)2 * scale * s));
     } else if (e < E2) {
       const int ia = (e - E1) / NC, ic = (e - E1) % NC;
       for (int ib = 0; ib < NB; ++ib)
-        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (b0 + ib) * n + d0 + id);
+        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * ldg_r(D + (b0 + ib) * n + d0 + id);
       atomicAdd(Kh + (a0 + ia) * n + c0 + ic, to_f64(scale * s));
     } else if (e < E3) {
       const int ib = (e - E2) / NC, ic = (e - E2) % NC;
       for (int ia = 0; ia < NA; ++ia)
-        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + d0 + id);
+        for (int id = 0; id < ND; ++id) s += V4(ia, ib, ic, id) * ldg_r(D + (a0 + ia) * n + d0 + id);
       atomicAdd(Kh + (b0 + ib) * n + c0 + ic, to_f64(scale * s));
     } else if (e < E4) {
       const int ia = (e - E3) / ND, id = (e - E3) % ND;
       for (int ib = 0; ib < NB; ++ib)
-        for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * __ldg(D + (b0 + ib) * n + c0 + ic);
+        for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * ldg_r(D + (b0 + ib) * n + c0 + ic);
       atomicAdd(Kh + (a0 + ia) * n + d0 + id, to_f64(scale * s));
     } else {
       const int ib = (e - E4) / ND, id = (e - E4) % ND;
       for (int ia = 0; ia < NA; ++ia)
-        for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * __ldg(D + (a0 + ia) * n + c0 + ic);
+        for (int ic = 0; ic < NC; ++ic) s += V4(ia, ib, ic, id) * ldg_r(D + (a0 + ia) * n + c0 + ic);
       atomicAdd(Kh + (b0 + ib) * n + d0 + id, to_f64(scale * s));
     }
   }
@@ -616,18 +759,23 @@ struct ClassWork {
   int64_t n;
   int x0, y0;              // first global pair index of class X / Y
   int same;                // X == Y
-  int psplit;              // P: primitive sub-groups per quartet (T*P <= 32)
+  int psplit;              // P: primitive sub-groups per quartet inside one group of T*P <= 32 lanes
+  int wsplit;              // W: groups per quartet; group c of W runs primitive sub-groups c*P .. c*P+P-1
+                           // of W*P and digests its partial integrals itself (digestion is linear)
 };
 
 constexpr int kBlock = 128;
+constexpr int kMaxWsplit = 64;
 
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, const R *__restrict__ D, double *Jh,
                                                     double *Kh) {
-  const int P = w.psplit;
+  const int P = w.psplit, W = w.wsplit;
   const int TP = T * P;
   const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
-  const int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp;
+  const int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;
+  const int64_t q = gid / W;
+  const int sub = (int)(gid - q * W) * P + p;   // primitive sub-group of the W*P
   if (q >= w.n) return;
   const int2 ij = __ldg(w.list + q);
   const int i = ij.x, j = ij.y;
@@ -641,7 +789,7 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
   const unsigned qmask = (TP == 32) ? 0xffffffffu : (((1u << TP) - 1u) << (lane & ~(TP - 1)));
   if constexpr (T == 1) {
     R acc[QC<LA, LB, LC, LD>::NABCD];
-    eval_t1<LA, LB, LC, LD, R>(kp, g, acc, p, P);
+    eval_t1<LA, LB, LC, LD, R>(kp, g, acc, sub, W * P);
     if (P > 1) reduce_psplit<R, QC<LA, LB, LC, LD>::NABCD, 1>(acc, P, qmask);
     if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh);
   } else {
@@ -650,7 +798,7 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
     R *buf = reinterpret_cast<R *>(smem_raw) + (threadIdx.x / T) * GP::BUFN;
     const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
     R acc[GP::NPER];
-    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc, p, P);
+    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc, sub, W * P);
     if (P > 1) reduce_psplit<R, GP::NPER, T>(acc, P, qmask);
     if (p == 0) digest_grp<LA, LB, LC, LD, R, T>(kp, g, acc, buf, t, gmask, scale, D, Jh, Kh);
   }
@@ -666,32 +814,40 @@ struct EriWork {
   const int *strides;          // 4 output strides per quartet (canonical slot order)
   int64_t n;
   double *out;
+  int psplit;                  // P primitive sub-groups per quartet (T*P <= 32)
 };
 
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __global__ void __launch_bounds__(kBlock) eri_kernel(KParams kp, EriWork w) {
   using Q = QC<LA, LB, LC, LD>;
-  constexpr int G = kBlock / T;
-  const int grp = threadIdx.x / T, t = threadIdx.x % T;
-  const int64_t q = (int64_t)blockIdx.x * G + grp;
+  const int P = w.psplit;
+  const int TP = T * P;
+  const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
+  const int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp;
   if (q >= w.n) return;
   const int fl = w.flags[q];
   const QGeom<R> g = make_geom<R>(kp, w.pab[q], w.pcd[q], fl & 1, fl & 2);
   const int s0 = w.strides[4 * q], s1 = w.strides[4 * q + 1], s2 = w.strides[4 * q + 2], s3 = w.strides[4 * q + 3];
   double *out = w.out + w.out_off[q];
+  const int lane = threadIdx.x & 31;
+  const unsigned qmask = (TP == 32) ? 0xffffffffu : (((1u << TP) - 1u) << (lane & ~(TP - 1)));
   if constexpr (T == 1) {
     R acc[Q::NABCD];
-    eval_t1<LA, LB, LC, LD, R>(kp, g, acc);
+    eval_t1<LA, LB, LC, LD, R>(kp, g, acc, p, P);
+    if (P > 1) reduce_psplit<R, Q::NABCD, 1>(acc, P, qmask);
+    if (p != 0) return;
 #pragma unroll
     for (int o = 0; o < Q::NABCD; ++o)
       out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = to_f64(acc[o] * (R)Q::norm(o));
   } else {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using GP = Grp<LA, LB, LC, LD, R, T>;
-    R *buf = reinterpret_cast<R *>(smem_raw) + grp * GP::BUFN;
-    const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1)));
+    R *buf = reinterpret_cast<R *>(smem_raw) + (threadIdx.x / T) * GP::BUFN;
+    const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
     R acc[GP::NPER];
-    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc);
+    eval_grp<LA, LB, LC, LD, R, T>(kp, g, buf, t, gmask, acc, p, P);
+    if (P > 1) reduce_psplit<R, GP::NPER, T>(acc, P, qmask);
+    if (p != 0) return;
 #pragma unroll
     for (int k = 0; k < GP::NPER; ++k) {
       const int o = t + k * T;

@@ -40,6 +40,21 @@ __host__ __device__ constexpr int rys_tab_offset(int n, int deg) {
 }
 __host__ __device__ constexpr int rys_tab_size(int deg) { return rys_tab_offset(kMaxRoots + 1, deg); }
 
+// Layout of the FP32 table read by the kernels: per n-root block, interval j,
+// root r, one row of kTab32Row floats holding the coefficient pairs
+// (u_k, w_k) from k = kTabDeg32 down to 0 (the Horner order): one root costs
+// kTabDeg32+1 eight-byte loads of one contiguous row (no padding: the
+// kernels that read it are bound by L1 bytes).
+constexpr int kTab32Row = 2 * (kTabDeg32 + 1);
+__host__ __device__ constexpr int rys_tab32v_offset(int n) { return kTabNint * kTab32Row * ((n - 1) * n / 2); }
+__host__ __device__ constexpr int rys_tab32v_size() { return rys_tab32v_offset(kMaxRoots + 1); }
+
+// Layout of the double-float copy of the FP64 table (in 16-byte units): per
+// n-root block, interval j, root r, the kTabDeg64+1 coefficients from
+// k = kTabDeg64 down to 0, each (u_hi, u_lo, w_hi, w_lo).
+__host__ __device__ constexpr int rys_tabdd_offset(int n) { return kTabNint * (kTabDeg64 + 1) * ((n - 1) * n / 2); }
+__host__ __device__ constexpr int rys_tabdd_size() { return rys_tabdd_offset(kMaxRoots + 1); }
+
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 __host__ __device__ constexpr int pair_class_of(int la, int lb) {  // la >= lb
   return la * (la + 1) / 2 + lb;
@@ -83,6 +98,10 @@ struct DevPrims {
 struct RysAsym {
   double r[kMaxRoots + 1][kMaxRoots];   // u_i * x as x -> inf
   double w[kMaxRoots + 1][kMaxRoots];   // w_i * sqrt(x) as x -> inf
+};
+struct RysAsym32 {                      // the same constants rounded to FP32
+  float r[kMaxRoots + 1][kMaxRoots];
+  float w[kMaxRoots + 1][kMaxRoots];
 };
 
 // host-side: build tables (rys_table.cpp)

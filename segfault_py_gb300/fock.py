@@ -150,6 +150,50 @@ class FockBuilder:
         torch.cuda.synchronize()
         return g
 
+    def autotune(self, D: torch.Tensor, precision: str | None = None, cutoff: float | None = None,
+                 fp32_cutoff: float | None = None, reps: int = 3):
+        """Time candidate primitive splits of every launch of a Fock build at
+        these settings and keep the fastest (sf_autotune); returns the table."""
+        prec = _lib.PRECISION[precision or self.precision]
+        if D.shape != (self.nao, self.nao) or D.dtype != torch.float64 or D.device != self.device:
+            raise ValueError("D must be a (%d,%d) float64 tensor on %s" % (self.nao, self.nao, self.device))
+        D = D.contiguous()
+        with torch.cuda.device(self.device):
+            rc = _lib.lib().sf_autotune(self._h, _ptr(D), prec, self.cutoff if cutoff is None else cutoff,
+                                        self.fp32_cutoff if fp32_cutoff is None else fp32_cutoff, int(reps),
+                                        _stream_ptr())
+        if rc < 0:
+            _lib.check(rc)
+        return self.tuning()
+
+    def tuning(self):
+        """The recorded launch splits: list of dicts (cls, precision, cost, split, ms_default, ms_tuned)."""
+        L = _lib.lib()
+        out = []
+        for i in range(L.sf_tuning_count(self._h)):
+            e = _lib.TuneEntry()
+            _lib.check(L.sf_get_tuning(self._h, i, C.byref(e)))
+            out.append(e.as_dict())
+        return out
+
+    def set_tuning(self, table):
+        """Load a table returned by `tuning()` (e.g. read back from JSON)."""
+        arr = (_lib.TuneEntry * max(len(table), 1))()
+        for i, e in enumerate(table):
+            arr[i] = _lib.TuneEntry(int(e["cls"]), int(e["precision"]), int(e["cost"]), int(e["split"]),
+                                    float(e.get("ms_default", 0.0)), float(e.get("ms_tuned", 0.0)))
+        _lib.check(_lib.lib().sf_set_tuning(self._h, arr, len(table)))
+
+    def save_tuning(self, path: str):
+        import json
+        with open(path, "w") as f:
+            json.dump({"nao": self.nao, "entries": self.tuning()}, f, indent=1)
+
+    def load_tuning(self, path: str):
+        import json
+        with open(path) as f:
+            self.set_tuning(json.load(f)["entries"])
+
     def set_profiling(self, on=True):
         """True/1: time every class launch; 2: also serialise the launches on
         the caller's stream so each time is the kernel alone."""
@@ -171,22 +215,21 @@ class FockBuilder:
         return H + J - 0.5 * K
 
     # ------------------------------------------------------------------
+    def eri_plan(self, quartets) -> "EriPlan":
+        """Prepare a raw-ERI batch of shell quartets (nq,4) for repeated runs."""
+        return EriPlan(self, quartets)
+
     def eri_quartets(self, quartets, precision: str = "fp64"):
         """Contracted integrals of shell quartets (nq,4): list of (na,nb,nc,nd) arrays."""
         q = np.ascontiguousarray(quartets, dtype=np.int32).reshape(-1, 4)
         nc = (self.l + 1) * (self.l + 2) // 2
+        plan = self.eri_plan(q)
+        try:
+            flat = plan.run(precision).cpu().numpy()
+            offs = plan.offsets
+        finally:
+            plan.close()
         sizes = np.prod(nc[q], axis=1).astype(np.int64)
-        offs = np.zeros(len(q), dtype=np.int64)
-        if len(q):
-            offs[1:] = np.cumsum(sizes)[:-1]
-        total = int(sizes.sum())
-        dq = torch.from_numpy(q).to(self.device)
-        do = torch.from_numpy(offs).to(self.device)
-        out = torch.zeros(max(total, 1), dtype=torch.float64, device=self.device)
-        with torch.cuda.device(self.device):
-            _lib.check(_lib.lib().sf_eri_batch(self._h, _ptr(dq), len(q), _lib.PRECISION[precision], _ptr(out),
-                                               _ptr(do), _stream_ptr()))
-        flat = out.cpu().numpy()
         return [flat[o:o + s].reshape(tuple(nc[row])) for o, s, row in zip(offs, sizes, q)]
 
     def build_eri(self, precision: str = "fp64") -> np.ndarray:
@@ -230,6 +273,50 @@ class FockBuilder:
             _lib.check(_lib.lib().sf_one_electron(self._h, _ptr(xyz), _ptr(Z), len(Z), _ptr(S), _ptr(T), _ptr(V),
                                                   _stream_ptr()))
         return S, T, V
+
+
+class EriPlan:
+    """A raw-ERI batch (sf_eri_plan): the quartets are canonicalised, grouped
+    by class and cost-sorted once; ``run`` evaluates all of them (FP64 or FP32,
+    stored as float64) into one packed device vector, quartet q at
+    ``offsets[q]`` in row-major (a, b, c, d) component order."""
+
+    def __init__(self, fb: FockBuilder, quartets):
+        q = np.ascontiguousarray(quartets, dtype=np.int32).reshape(-1, 4)
+        self.fb = fb
+        self.nq = len(q)
+        h = C.c_void_p()
+        with torch.cuda.device(fb.device):
+            _lib.check(_lib.lib().sf_eri_plan_create(fb.handle, q.ctypes.data, self.nq, C.byref(h)))
+        self._p = h
+        outs, prims, flops = C.c_int64(), C.c_int64(), C.c_double()
+        _lib.check(_lib.lib().sf_eri_plan_info(self._p, C.byref(outs), C.byref(prims), C.byref(flops)))
+        self.outputs, self.prim_quartets, self.flop_alg = outs.value, prims.value, flops.value
+        self.offsets = np.zeros(self.nq, dtype=np.int64)
+        _lib.check(_lib.lib().sf_eri_plan_offsets(self._p, self.offsets.ctypes.data))
+
+    def run(self, precision: str = "fp64", out: torch.Tensor | None = None) -> torch.Tensor:
+        if precision not in ("fp64", "fp32", "df"):
+            raise ValueError("precision must be fp64, fp32 or df")
+        if out is None:
+            out = torch.empty(max(self.outputs, 1), dtype=torch.float64, device=self.fb.device)
+        elif out.dtype != torch.float64 or out.numel() < self.outputs or not out.is_contiguous():
+            raise ValueError("out must be a contiguous float64 tensor of >= %d values" % self.outputs)
+        with torch.cuda.device(self.fb.device):
+            _lib.check(_lib.lib().sf_eri_plan_run(self._p, _lib.PRECISION[precision], _ptr(out), _stream_ptr()))
+        return out
+
+    def close(self):
+        if getattr(self, "_p", None):
+            with torch.cuda.device(self.fb.device):
+                _lib.lib().sf_eri_plan_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _comp_factor(shell) -> float:

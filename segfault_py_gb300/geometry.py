@@ -110,3 +110,26 @@ def random_quartet_shells(nshell: int, seed: int = 0, lmax: int = 2, kmax: int =
     po[1:] = np.cumsum(nprim)
     return dict(l=ls, nprim=nprim, atom=np.arange(nshell, dtype=np.int32), ao_offset=ao,
                 center=np.array(cen), prim_offset=po, exps=np.concatenate(exps), coefs=np.concatenate(coefs))
+
+
+PAIR_L = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]
+QUARTET_CLASSES = [(PAIR_L[x], PAIR_L[y]) for x in range(6) for y in range(x + 1)]
+
+
+def random_quartet_batch(nq: int, nshell: int = 600, seed: int = 0, kmax: int = 6, box: float = 10.0):
+    """Raw-ERI stress batch: a pool of `nshell` random shells
+    (random_quartet_shells: contraction 1..kmax, exponents log-uniform in
+    [0.05, 1e4], normalised, centres uniform in a `box` A cube) and `nq` shell
+    quartets whose canonical class is uniform over the 21 classes ss|ss ..
+    dd|dd.  Returns (shell table, int32 (nq, 4) quartets)."""
+    table = random_quartet_shells(nshell, seed=seed, kmax=kmax, box=box)
+    rng = np.random.default_rng(seed + 1)
+    ls = table["l"]
+    byl = [np.where(ls == l)[0] for l in range(3)]
+    cls = rng.integers(0, len(QUARTET_CLASSES), nq)
+    q = np.empty((nq, 4), dtype=np.int32)
+    for k, ((la, lb), (lc, ld)) in enumerate(QUARTET_CLASSES):
+        sel = np.where(cls == k)[0]
+        for col, l in enumerate((la, lb, lc, ld)):
+            q[sel, col] = rng.choice(byl[l], len(sel))
+    return table, q

@@ -39,7 +39,7 @@ def slice_table(fb: FockBuilder):
     rows = []
     for q in sorted(sl, key=lambda q: -q["ms"]):
         rows.append("(%d%d|%d%d) %s T=%2d q=%9d pq=%11d ms=%8.4f share=%5.1f%% GF/s=%8.1f" % (
-            q["la"], q["lb"], q["lc"], q["ld"], "f64" if q["precision"] == 0 else "f32",
+            q["la"], q["lb"], q["lc"], q["ld"], ("f64", "f32", "dd")[q["precision"]],
             q["threads_per_quartet"], q["quartets"], q["prim_quartets"], q["ms"],
             100.0 * q["ms"] / max(tot, 1e-30), q["flop_alg"] / max(q["ms"], 1e-30) / 1e6))
     return tot, rows
@@ -49,11 +49,12 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--nwater", type=int, default=8)
     ap.add_argument("--basis", default="6-31g*")
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "fp32", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "fp32", "mixed", "mixed_df", "df"])
     ap.add_argument("--cutoff", type=float, default=1e-12)
     ap.add_argument("--fp32-cutoff", type=float, default=1e-2)
     ap.add_argument("--builds", type=int, default=3)
     ap.add_argument("--slices", action="store_true")
+    ap.add_argument("--time", action="store_true", help="also time --builds normal (concurrent) builds with events")
     a = ap.parse_args(argv)
     preload_torch_linalg()
     sym, xyz = geometry.water_cluster(a.nwater)
@@ -70,6 +71,19 @@ def main(argv=None):
         tot, rows = slice_table(fb)
         print("serialised kernel time of one build: %.4f ms" % tot)
         print("\n".join(rows))
+    if a.time:
+        fb.set_profiling(0)
+        J = torch.empty_like(D)
+        K = torch.empty_like(D)
+        for _ in range(3):
+            fb.jk(D, out=(J, K))
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(a.builds):
+            fb.jk(D, out=(J, K))
+        ev[1].record()
+        torch.cuda.synchronize()
+        print("wall time of one build (mean of %d back to back): %.4f ms" % (a.builds, ev[0].elapsed_time(ev[1]) / a.builds))
 
 
 if __name__ == "__main__":

@@ -56,7 +56,7 @@ def test_eri_rys_shim_matches_reference(cuda, quartet_golden):
         assert abs(v - e["value"]) <= 1e-12 * max(1.0, abs(e["value"])) + 1e-11 * abs(e["value"])
 
 
-@pytest.mark.parametrize("precision,rtol,gtol", [("fp64", 1e-10, 1e-14), ("fp32", 1e-4, 1e-7)])
+@pytest.mark.parametrize("precision,rtol,gtol", [("fp64", 1e-10, 1e-14), ("fp32", 1e-4, 1e-7), ("df", 1e-10, 1e-14)])
 def test_all_classes_random_shells_vs_oracle(cuda, precision, rtol, gtol):
     """Every (la,lb,lc,ld) order of l <= 2 on random contracted shells
     (exponents up to 1e4).  Reference: the oracle with exact Rys roots.  The
@@ -66,7 +66,8 @@ def test_all_classes_random_shells_vs_oracle(cuda, precision, rtol, gtol):
     of the whole set (quartets that underflow).  FP32: the horizontal transfer
     I(a,b+1) = I(a+1,b) + AB I(a,b) over |AB| up to 12 bohr amplifies the
     single-precision rounding of cancelling terms (observed 5e-5 of the quartet
-    maximum for a distant d pair), hence 1e-4 and 1e-7."""
+    maximum for a distant d pair), hence 1e-4 and 1e-7.  Double-float
+    (FP32 pairs, ~2^-44 per operation) is held to the FP64 bound."""
     from segfault_py_gb300 import geometry as G
     table = G.random_quartet_shells(40, seed=11, kmax=4, box=4.0)
     rng = np.random.default_rng(5)
@@ -141,6 +142,10 @@ def test_jk_vs_oracle(cuda, basis):
     J32, K32 = fb.jk(torch.tensor(D, device=cuda), precision="fp32")
     assert np.abs(J32.cpu().numpy() - Jo).max() < 3e-6 * scale
     assert np.abs(K32.cpu().numpy() - Ko).max() < 3e-6 * scale
+    # double-float quartets: FP64-class accuracy (2^-44 per operation)
+    Jd, Kd = fb.jk(torch.tensor(D, device=cuda), precision="df")
+    assert np.abs(Jd.cpu().numpy() - Jo).max() < 1e-11 * scale
+    assert np.abs(Kd.cpu().numpy() - Ko).max() < 1e-11 * scale
 
 
 def test_screened_quartet_count_matches_rule(cuda):
@@ -215,8 +220,11 @@ def test_mixed_precision_energy_error(cuda):
         J, K = fb.jk(D, precision=prec)
         F = H + J - 0.5 * K
         return float(0.5 * torch.sum(D * (H + F)))
-    e64, emx = energy("fp64"), energy("mixed")
+    e64, emx, edf = energy("fp64"), energy("mixed"), energy("mixed_df")
     assert abs(emx - e64) < 1e-6
+    # FP32 below the cutoff, double-float above: the same error budget
+    assert abs(edf - e64) < 1e-6
+    assert abs(energy("df") - e64) < 1e-9
 
 
 def test_partition_slices_sum_to_full(cuda):
@@ -239,3 +247,38 @@ def test_partition_slices_sum_to_full(cuda):
     scale = float(max(J.abs().max(), K.abs().max()))
     assert float((Js - J).abs().max()) < 1e-12 * scale
     assert float((Ks - K).abs().max()) < 1e-12 * scale
+
+
+def test_autotune_keeps_results(cuda, tmp_path):
+    """The autotuner only changes how a quartet's primitive loop is split over
+    lanes: J and K after tuning agree with the untuned build to summation-order
+    rounding, the table survives a JSON round trip, and clearing it restores the
+    rule's launches."""
+    import torch
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.molecule import Molecule
+    sym, xyz = G.water_cluster(2)
+    mol = Molecule.from_geometry(sym, xyz, "6-31g*")
+    fb = FockBuilder(mol, device=cuda, fp32_cutoff=1e-2)
+    torch.manual_seed(0)
+    A = torch.randn(mol.nao, mol.nao, dtype=torch.float64, device=cuda)
+    D = (A + A.T) / mol.nao
+    for prec in ("fp64", "mixed"):
+        J0, K0 = fb.jk(D, precision=prec)
+        table = fb.autotune(D, precision=prec, reps=2)
+        assert len(table) > 0
+        assert all(e["split"] >= 1 and (e["split"] & (e["split"] - 1)) == 0 for e in table)
+        J1, K1 = fb.jk(D, precision=prec)
+        tol = 1e-12 if prec == "fp64" else 1e-6
+        assert float((J1 - J0).abs().max()) <= tol * float(J0.abs().max())
+        assert float((K1 - K0).abs().max()) <= tol * float(K0.abs().max())
+    path = str(tmp_path / "tune.json")
+    fb.save_tuning(path)
+    saved = fb.tuning()
+    fb.set_tuning([])
+    assert fb.tuning() == []
+    fb.load_tuning(path)
+    assert [(e["cls"], e["precision"], e["cost"], e["split"]) for e in fb.tuning()] == \
+           [(e["cls"], e["precision"], e["cost"], e["split"]) for e in saved]
+    fb.close()

@@ -13,23 +13,9 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-PAIR_L = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]
-CLASSES = [(PAIR_L[x], PAIR_L[y]) for x in range(6) for y in range(x + 1)]
-
-
 def stress_quartets(nq, nshell=600, seed=0):
     from segfault_py_gb300 import geometry as G
-    table = G.random_quartet_shells(nshell, seed=seed, kmax=6, box=10.0)
-    rng = np.random.default_rng(seed + 1)
-    ls = table["l"]
-    byl = [np.where(ls == l)[0] for l in range(3)]
-    cls = rng.integers(0, 21, nq)
-    q = np.empty((nq, 4), dtype=np.int32)
-    for k, ((la, lb), (lc, ld)) in enumerate(CLASSES):
-        sel = np.where(cls == k)[0]
-        for col, l in enumerate((la, lb, lc, ld)):
-            q[sel, col] = rng.choice(byl[l], len(sel))
-    return table, q
+    return G.random_quartet_batch(nq, nshell=nshell, seed=seed)
 
 
 def _oracle_block(table, q):
@@ -61,3 +47,39 @@ def test_stress_batch_sampled_vs_oracle(cuda, precision, rtol, gtol):
         assert np.all(np.isfinite(blk))
         assert np.abs(blk - ref).max() <= rtol * np.abs(ref).max() + gtol * gmax, (q[s].tolist(),)
     fb.close()
+
+
+def test_eri_plan_matches_batch_with_offsets(cuda):
+    """sf_eri_plan (packed outputs) against sf_eri_batch with caller-chosen
+    offsets (blocks stored in reverse order); both FP64 and FP32; the packed
+    offsets are the running sums of the block sizes."""
+    import ctypes as C
+    import torch
+    from segfault_py_gb300 import _lib
+    from segfault_py_gb300.fock import FockBuilder
+    table, q = stress_quartets(20_000, seed=3)
+    fb = FockBuilder(table, device=cuda)
+    nc = (fb.l + 1) * (fb.l + 2) // 2
+    sizes = np.prod(nc[q], axis=1).astype(np.int64)
+    plan = fb.eri_plan(q)
+    assert plan.outputs == int(sizes.sum())
+    assert np.array_equal(plan.offsets[1:], np.cumsum(sizes)[:-1]) and plan.offsets[0] == 0
+    assert plan.prim_quartets == int(np.sum(table["nprim"][q].prod(axis=1)))
+    rev = np.zeros(len(q), dtype=np.int64)
+    rev[::-1] = np.concatenate([[0], np.cumsum(sizes[::-1])[:-1]])
+    dq = torch.from_numpy(q).to(cuda)
+    do = torch.from_numpy(rev).to(cuda)
+    for prec in ("fp64", "fp32"):
+        packed = plan.run(prec).cpu().numpy()
+        again = plan.run(prec).cpu().numpy()
+        assert np.array_equal(packed, again)
+        out = torch.zeros(plan.outputs, dtype=torch.float64, device=cuda)
+        _lib.check(_lib.lib().sf_eri_batch(fb.handle, C.c_void_p(dq.data_ptr()), len(q), _lib.PRECISION[prec],
+                                           C.c_void_p(out.data_ptr()), C.c_void_p(do.data_ptr()),
+                                           C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        o = out.cpu().numpy()
+        for k in range(0, len(q), 97):
+            a = packed[plan.offsets[k]:plan.offsets[k] + sizes[k]]
+            b = o[rev[k]:rev[k] + sizes[k]]
+            assert np.array_equal(a, b), k
+    plan.close()
