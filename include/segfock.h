@@ -134,15 +134,22 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
  * T x P x W lanes: T lanes share its Cartesian outputs (fixed per class),
  * its primitive loop is split S = P*W ways (P lane groups inside a warp, W
  * separate groups whose partial integrals are digested separately).  The
- * library picks S by a cost rule; sf_autotune times, for every launch of the
- * given precision and cutoffs, S/4, S/2, S, 2S, 4S on `stream` (each candidate
- * reps times, launches serialised, adding into the handle's scratch only),
- * keeps the fastest and records it; later builds with the same work lists use
- * the recorded splits.  Returns the number of launches tuned (>= 0) or an
- * error code.  The table can be read out and loaded again (e.g. from a file):
- * sf_set_tuning replaces it (n = 0 clears it). */
+ * library picks S by a cost rule: enough sub-groups that a launch covers
+ * the GPU ("fill" target), at least one primitive quartet each.  sf_autotune,
+ * for the given precision mode and cutoffs, on `stream` (adding into the
+ * handle's scratch only; the caller's matrices are not touched):
+ *   1. times whole builds (launches concurrent) with fill targets 0, 1/4, 1
+ *      and 4 times 8 warps per SM sub-partition and keeps the fastest;
+ *   2. times every launch alone (reps times) with S/4, S/2, S, 2S, 4S and
+ *      records the fastest; streams are then assigned by measured times;
+ *   3. keeps the step-2 splits only if the whole build got faster.
+ * Later builds with the same work lists use the recorded shapes.  Returns the
+ * number of launches tuned (>= 0) or an error code.  The table can be read
+ * out and loaded again (e.g. from a file): sf_set_tuning replaces it (n = 0
+ * clears it).  Entries with cls = -1 hold the fill target of precision mode
+ * `precision` in `split` (quarters; 0 = no extra split). */
 typedef struct {
-    int32_t cls;           /* canonical class 0..20 (ss|ss .. dd|dd)          */
+    int32_t cls;           /* canonical class 0..20 (ss|ss .. dd|dd); -1: fill target */
     int32_t precision;     /* launch kind: 0 FP64, 1 FP32, 2 double-float     */
     int64_t cost;          /* K_ab*K_cd of the launch's first (costliest) quartet */
     int32_t split;         /* chosen S = P*W (power of two)                   */

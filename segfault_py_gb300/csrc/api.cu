@@ -209,7 +209,7 @@ struct sf_handle {
   // side streams: the class launches of one build are independent (they only
   // add into Jh/Kh with atomics), so they are spread over kSideStreams
   // streams forked from and joined back into the caller's stream
-  static constexpr int kSideStreams = 8;
+  static constexpr int kSideStreams = 16;
   cudaStream_t side[kSideStreams] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[kSideStreams] = {};
   std::vector<int> slice_stream;   // side stream of each slice (greedy by cost)
@@ -220,6 +220,9 @@ struct sf_handle {
   int64_t st_q[2] = {0, 0}, st_pq[2] = {0, 0}, st_total = 0;
   double st_f[2] = {0, 0};
   int part = 0, nparts = 1;
+  // launch-fill target per precision mode, in quarters of "8 resident warps
+  // per SM sub-partition" (0: no extra primitive split); set by sf_autotune
+  int fill_x4[5] = {4, 4, 4, 4, 4};
   KParams kp;
 };
 
@@ -408,7 +411,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       // sub-partition's FP64 unit for 64 cycles): its quartets' primitive
       // loops are split further, up to S_fill = P*W sub-groups per quartet,
       // each sub-group keeping at least one primitive quartet
-      const int64_t fill = (int64_t)std::max(h->nsm, 1) * 4 * 8 * 32;
+      const int64_t fill = (int64_t)std::max(h->nsm, 1) * 4 * 8 * 32 * h->fill_x4[prec] / 4;
       int sfill = 1;
       while (p.n * T * sfill < fill && sfill < pmax * kMaxWsplit) sfill *= 2;
       auto split_of = [&](int64_t cost) {
@@ -468,6 +471,21 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       const double nc = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
       cost[k] = (double)sl.prims * (nr * (nc + 30.0) + 40.0) * (sl.prec == 0 ? 16.0 : sl.prec == 2 ? 5.0 : 1.0);
     }
+    // launches timed by the autotuner: their measured times (a latency-bound
+    // launch of few quartets costs far more than its work suggests)
+    bool all_timed = !h->slices.empty();
+    std::vector<double> timed(h->slices.size(), 0.0);
+    for (size_t k = 0; k < h->slices.size() && all_timed; ++k) {
+      const auto &sl = h->slices[k];
+      bool found = false;
+      for (const sf_tune_entry &e : h->tune)
+        if (e.cls == sl.cls && e.precision == sl.prec && e.cost == sl.cost_hi && e.ms_tuned > 0.f) {
+          timed[k] = e.ms_tuned;
+          found = true;
+        }
+      all_timed = found;
+    }
+    if (all_timed) cost = timed;
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
     std::vector<sf_handle::Slice> sorted;
@@ -1071,6 +1089,67 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
     *ms /= (float)reps;
     return e;
   };
+  // whole-build time of the current lists, launches concurrent as in a build
+  auto time_build = [&](float *ms) -> int {
+    int r2 = build_work(h, precision, cutoff, fp32_cutoff);
+    if (r2) return r2;
+    r2 = launch_slices(h, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st, 0, nullptr);   // warm-up
+    if (r2) return r2;
+    SF_CK(cudaEventRecord(e0, st));
+    for (int r = 0; r < reps; ++r) {
+      r2 = launch_slices(h, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st, 0, nullptr);
+      if (r2) return r2;
+    }
+    SF_CK(cudaEventRecord(e1, st));
+    SF_CK(cudaEventSynchronize(e1));
+    SF_CK(cudaEventElapsedTime(ms, e0, e1));
+    *ms /= (float)reps;
+    return SF_OK;
+  };
+  auto drop_entries = [&]() {
+    std::vector<sf_tune_entry> keep;
+    const int kinds[2] = {(precision == SF_PREC_MIXED_DF || precision == SF_PREC_DF) ? 2 : 0, 1};
+    for (const auto &x : h->tune) {
+      bool mine = x.cls == -1 ? x.precision == precision : false;
+      if (x.cls >= 0)
+        for (int k : kinds)
+          if (x.precision == k &&
+              ((k == 1 && precision != SF_PREC_FP64 && precision != SF_PREC_DF) ||
+               (k != 1 && precision != SF_PREC_FP32)))
+            mine = true;
+      if (!mine) keep.push_back(x);
+    }
+    h->tune.swap(keep);
+  };
+  // 1. the launch-fill target of this mode, by whole-build time (per-launch
+  // splits of this mode cleared first)
+  drop_entries();
+  int best_fill = h->fill_x4[precision];
+  float best_ms = 1e30f;
+  for (int f : {0, 1, 4, 16}) {
+    h->fill_x4[precision] = f;
+    h->c_prec = -1;
+    float ms = 0.f;
+    rc = time_build(&ms);
+    if (rc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_fill = f;
+    }
+  }
+  h->fill_x4[precision] = best_fill;
+  h->c_prec = -1;
+  rc = build_work(h, precision, cutoff, fp32_cutoff);
+  if (rc) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
+  // 2. per-launch splits, each launch timed alone
   int tuned = 0;
   for (auto &sl : h->slices) {
     const ClassInfo &ci = kClassInfo[sl.cls];
@@ -1111,8 +1190,24 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
     if (!found) h->tune.push_back(te);
     ++tuned;
   }
+  // 3. keep the per-launch splits (and the stream assignment by their
+  // measured times) only if the whole build got faster
+  h->c_prec = -1;
+  float tuned_ms = 0.f;
+  rc = time_build(&tuned_ms);
+  if (rc) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
+  if (tuned_ms > best_ms) {
+    drop_entries();
+    tuned = 0;
+  }
+  h->tune.push_back(sf_tune_entry{-1, precision, 0, best_fill, best_ms, std::min(best_ms, tuned_ms)});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  h->c_prec = -1;   // the next build re-cuts the lists and assigns streams by the measured times
   return tuned;
 }
 
@@ -1128,11 +1223,17 @@ int sf_set_tuning(sf_handle *h, const sf_tune_entry *entries, int32_t n) {
   if (!h || n < 0 || (n > 0 && !entries)) return fail(SF_EINVAL, "sf_set_tuning: bad arguments");
   for (int32_t i = 0; i < n; ++i) {
     const sf_tune_entry &e = entries[i];
+    const bool fill_entry = e.cls == -1 && e.precision >= 0 && e.precision <= SF_PREC_DF && e.split >= 0 &&
+                            e.split <= 64;
+    if (fill_entry) continue;
     if (e.cls < 0 || e.cls >= kNumClass || e.precision < 0 || e.precision > 2 || e.split < 1 ||
         e.split > 32 * kMaxWsplit || (e.split & (e.split - 1)))
       return fail(SF_EINVAL, "sf_set_tuning: bad entry " + std::to_string(i));
   }
   h->tune.assign(entries, entries + n);
+  for (int m = 0; m <= SF_PREC_DF; ++m) h->fill_x4[m] = 4;
+  for (const auto &e : h->tune)
+    if (e.cls == -1) h->fill_x4[e.precision] = e.split;
   h->c_prec = -1;   // rebuild the launch list with the new splits
   return SF_OK;
 }

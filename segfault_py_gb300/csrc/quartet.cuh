@@ -138,12 +138,24 @@ __device__ __forceinline__ void rys_roots_all_f32(const KParams &kp, float x, fl
 // dd: the FP64 table's coefficients as dd rows: per n-root block, interval
 // j, root r, the (D+1) coefficients from k = D down to 0, each one 16-byte
 // (u_hi, u_lo, w_hi, w_lo); Horner in dd
+// The leading kDDTop coefficients (k = D .. D-kDDTop+1) are summed in plain
+// FP32: over every interval and root their terms add up to less than 5e-8 of
+// |c_0| (Chebyshev-fitted rows decay geometrically), so FP32 rounding there
+// stays below 1e-14 relative; the remaining rows run in dd.
+constexpr int kDDTop = 4;
 __device__ __forceinline__ void rys_row_dd(const float4 *row, dd s, dd &u, dd &w) {
   const float4 top = __ldg(row);
-  u = dd(top.x, top.y);
-  w = dd(top.z, top.w);
+  float uf = top.x, wf = top.z;
 #pragma unroll
-  for (int k = 1; k <= kTabDeg64; ++k) {
+  for (int k = 1; k < kDDTop; ++k) {
+    const float4 c = __ldg(row + k);
+    uf = fmaf(uf, s.hi, c.x);
+    wf = fmaf(wf, s.hi, c.z);
+  }
+  u = dd(uf);
+  w = dd(wf);
+#pragma unroll
+  for (int k = kDDTop; k <= kTabDeg64; ++k) {
     const float4 c = __ldg(row + k);
     u = dd_fma(u, s, dd(c.x, c.y));
     w = dd_fma(w, s, dd(c.z, c.w));

@@ -55,12 +55,17 @@ def main(argv=None):
     ap.add_argument("--builds", type=int, default=3)
     ap.add_argument("--slices", action="store_true")
     ap.add_argument("--time", action="store_true", help="also time --builds normal (concurrent) builds with events")
+    ap.add_argument("--autotune", action="store_true", help="autotune the launch shapes first")
     a = ap.parse_args(argv)
     preload_torch_linalg()
     sym, xyz = geometry.water_cluster(a.nwater)
     mol = Molecule.from_geometry(sym, xyz, a.basis)
     fb = FockBuilder(mol, cutoff=a.cutoff, fp32_cutoff=a.fp32_cutoff, precision=a.precision)
     D = guess_density(fb, mol.nelectron // 2)
+    if a.autotune:
+        tab = fb.autotune(D, reps=3)
+        gain = sum(e["ms_default"] - e["ms_tuned"] for e in tab)
+        print("autotuned %d launches, serialised time saved %.4f ms" % (len(tab), gain))
     if a.slices:
         fb.set_profiling(2)
     for _ in range(a.builds):

@@ -253,7 +253,8 @@ def test_autotune_keeps_results(cuda, tmp_path):
     """The autotuner only changes how a quartet's primitive loop is split over
     lanes: J and K after tuning agree with the untuned build to summation-order
     rounding, the table survives a JSON round trip, and clearing it restores the
-    rule's launches."""
+    rule's launches.  The table may hold no per-launch entries when they did
+    not make the whole build faster; the fill entry (cls -1) is always there."""
     import torch
     from segfault_py_gb300 import geometry as G
     from segfault_py_gb300.fock import FockBuilder
@@ -267,8 +268,8 @@ def test_autotune_keeps_results(cuda, tmp_path):
     for prec in ("fp64", "mixed"):
         J0, K0 = fb.jk(D, precision=prec)
         table = fb.autotune(D, precision=prec, reps=2)
-        assert len(table) > 0
-        assert all(e["split"] >= 1 and (e["split"] & (e["split"] - 1)) == 0 for e in table)
+        assert any(e["cls"] == -1 for e in table)
+        assert all(e["split"] >= 1 and (e["split"] & (e["split"] - 1)) == 0 for e in table if e["cls"] >= 0)
         J1, K1 = fb.jk(D, precision=prec)
         tol = 1e-12 if prec == "fp64" else 1e-6
         assert float((J1 - J0).abs().max()) <= tol * float(J0.abs().max())
