@@ -191,6 +191,16 @@ int sf_eri_plan_info(const sf_eri_plan *plan, int64_t *outputs, int64_t *prim_qu
 /* host int64[nq]: output offset of every quartet */
 int sf_eri_plan_offsets(const sf_eri_plan *plan, int64_t *offsets);
 int sf_eri_plan_run(sf_eri_plan *plan, int32_t precision, double *out, void *stream);
+/* The same plan evaluated by the McMurchie-Davidson engine instead of Rys
+ * quadrature (Hermite expansion coefficients, Boys function and Hermite
+ * Coulomb integrals R_tuv: module mmd of src/hf/core/core.f90:23-198, the
+ * reference's second integral engine): an independent cross-check of the
+ * production Rys kernels.  SF_PREC_FP64: everything on the CUDA cores in
+ * FP64.  SF_PREC_FP32: FP32 MD whose bra Hermite-to-Cartesian E contraction
+ * runs on the tcgen05 tensor cores (kind::tf32, three-pass hi/lo split for
+ * FP32 accuracy); synchronises the stream and returns SF_ECUDA if a bounded
+ * wait on the tensor cores timed out.  Other precisions: SF_EUNSUPPORTED. */
+int sf_eri_plan_run_md(sf_eri_plan *plan, int32_t precision, double *out, void *stream);
 void sf_eri_plan_destroy(sf_eri_plan *plan);
 
 /* One-electron matrices (device, nao*nao each): overlap S, kinetic T and

@@ -899,6 +899,8 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   SF_CK(prepare_jk_dd());
   SF_CK(prepare_eri());
   SF_CK(prepare_eri_dd());
+  SF_CK(prepare_md());
+  SF_CK(prepare_md_tc());
   SF_CK(prepare_grad_f64());
   SF_CK(prepare_grad_f32());
   *out = guard.release();
@@ -1418,6 +1420,33 @@ int sf_eri_plan_run(sf_eri_plan *pl, int32_t precision, double *out, void *strea
   if (pl->nq > 0 && !out) return fail(SF_EINVAL, "sf_eri_plan_run: NULL output");
   DeviceGuard g(pl->h->device);
   return run_eri_plan(pl, precision, out, (cudaStream_t)stream);
+}
+
+int sf_eri_plan_run_md(sf_eri_plan *pl, int32_t precision, double *out, void *stream) {
+  if (!pl) return fail(SF_EINVAL, "sf_eri_plan_run_md: NULL plan");
+  if (precision != SF_PREC_FP64 && precision != SF_PREC_FP32)
+    return fail(SF_EUNSUPPORTED, "sf_eri_plan_run_md: the MD engine runs in FP64 or FP32 (tensor cores)");
+  if (pl->nq > 0 && !out) return fail(SF_EINVAL, "sf_eri_plan_run_md: NULL output");
+  DeviceGuard g(pl->h->device);
+  sf_handle *h = pl->h;
+  cudaStream_t st = (cudaStream_t)stream;
+  const auto &segs = pl->segs[0];
+  if (segs.empty()) return SF_OK;
+  const bool tc = precision == SF_PREC_FP32;
+  if (tc) SF_CK(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), st));
+  int rc = fan_out_list(h, st, pl->seg_stream[0], [&](size_t k, cudaStream_t ss) {
+    const sf_eri_plan::Seg &sg = segs[k];
+    EriWork w{pl->d_pab.p + sg.off, pl->d_pcd.p + sg.off, pl->d_fl.p + sg.off, pl->d_off.p + sg.off,
+              pl->d_str.p + 4 * sg.off, sg.n, out, 1};
+    return tc ? launch_md_tc(sg.cls, h->kp, w, h->nsm, ss) : launch_md_eri(sg.cls, h->kp, w, ss);
+  });
+  if (rc || !tc) return rc;
+  // the tensor-core kernels bound every wait on their MMAs and flag a timeout
+  int flag = 0;
+  SF_CK(cudaMemcpyAsync(&flag, h->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SF_CK(cudaStreamSynchronize(st));
+  if (flag) return fail(SF_ECUDA, "sf_eri_plan_run_md: a tensor-core MMA wait timed out");
+  return SF_OK;
 }
 
 void sf_eri_plan_destroy(sf_eri_plan *pl) {

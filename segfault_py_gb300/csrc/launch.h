@@ -13,6 +13,12 @@ cudaError_t launch_jk_dd(int cls, const KParams &kp, const ClassWork &w, const d
 // raw integrals of one class (fp32: FP32 evaluation, else FP64)
 cudaError_t launch_eri(int cls, int fp32, const KParams &kp, const EriWork &w, cudaStream_t st);
 cudaError_t launch_eri_dd(int cls, const KParams &kp, const EriWork &w, cudaStream_t st);
+// raw integrals of one class by McMurchie-Davidson (FP64)
+cudaError_t launch_md_eri(int cls, const KParams &kp, const EriWork &w, cudaStream_t st);
+cudaError_t prepare_md();
+// the same with the bra E contraction on the tensor cores (FP32 MD, 3-pass TF32)
+cudaError_t launch_md_tc(int cls, const KParams &kp, const EriWork &w, int nsm, cudaStream_t st);
+cudaError_t prepare_md_tc();
 // Schwarz bounds of pair class pc (0..5) over pairs [p0, p0+n)
 cudaError_t launch_schwarz(int pc, const KParams &kp, int p0, int n, double *qout, cudaStream_t st);
 

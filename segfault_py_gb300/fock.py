@@ -295,15 +295,20 @@ class EriPlan:
         self.offsets = np.zeros(self.nq, dtype=np.int64)
         _lib.check(_lib.lib().sf_eri_plan_offsets(self._p, self.offsets.ctypes.data))
 
-    def run(self, precision: str = "fp64", out: torch.Tensor | None = None) -> torch.Tensor:
+    def run(self, precision: str = "fp64", out: torch.Tensor | None = None, engine: str = "rys") -> torch.Tensor:
+        """engine "rys" (production kernels) or "md" (McMurchie-Davidson: FP64 on the
+        CUDA cores, or FP32 with the bra E contraction on the tensor cores)."""
         if precision not in ("fp64", "fp32", "df"):
             raise ValueError("precision must be fp64, fp32 or df")
+        if engine not in ("rys", "md"):
+            raise ValueError("engine must be rys or md")
         if out is None:
             out = torch.empty(max(self.outputs, 1), dtype=torch.float64, device=self.fb.device)
         elif out.dtype != torch.float64 or out.numel() < self.outputs or not out.is_contiguous():
             raise ValueError("out must be a contiguous float64 tensor of >= %d values" % self.outputs)
+        fn = _lib.lib().sf_eri_plan_run if engine == "rys" else _lib.lib().sf_eri_plan_run_md
         with torch.cuda.device(self.fb.device):
-            _lib.check(_lib.lib().sf_eri_plan_run(self._p, _lib.PRECISION[precision], _ptr(out), _stream_ptr()))
+            _lib.check(fn(self._p, _lib.PRECISION[precision], _ptr(out), _stream_ptr()))
         return out
 
     def close(self):
