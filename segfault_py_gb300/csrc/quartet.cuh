@@ -452,6 +452,33 @@ __device__ __forceinline__ void load_prim_ab(const KParams &kp, const QGeom<R> &
   s.pax = px - g.Ax; s.pay = py - g.Ay; s.paz = pz - g.Az;
 }
 
+// one ket primitive-pair record held in registers (loaded an iteration ahead)
+template <typename R>
+struct KetRec {
+  R q, qx, qy, qz, kcd, i2q;
+};
+template <typename R>
+__device__ __forceinline__ void load_ket(const KParams &kp, const QGeom<R> &g, int iq, KetRec<R> &k) {
+  load_rec<R>(prims_of<R>(kp).rec + (size_t)(g.cd_off + iq) * kPrimRec, k.q, k.qx, k.qy, k.qz, k.kcd, k.i2q);
+}
+
+// primitive-quartet scalars from the bra values and a ket record
+template <typename R>
+__device__ __forceinline__ void set_prim_cd(const QGeom<R> &g, const KetRec<R> &k, PQ<R> &s, R p, R px, R py, R pz,
+                                            R kab) {
+  const R q = k.q, qx = k.qx, qy = k.qy, qz = k.qz, kcd = k.kcd;
+  s.i2q = k.i2q;
+  s.qcx = qx - g.Cx; s.qcy = qy - g.Cy; s.qcz = qz - g.Cz;
+  s.pqx = px - qx; s.pqy = py - qy; s.pqz = pz - qz;
+  const R rr = rsqrt_nr(p + q);
+  s.r2 = rr * rr;
+  s.aq = q * s.r2;
+  s.ap = p * s.r2;
+  const R rho = p * s.aq;
+  s.x = rho * (s.pqx * s.pqx + s.pqy * s.pqy + s.pqz * s.pqz);
+  s.pref = kab * kcd * rr;
+}
+
 template <typename R>
 __device__ __forceinline__ void load_prim_cd(const KParams &kp, const QGeom<R> &g, int iq, PQ<R> &s, R p, R px, R py,
                                              R pz, R kab) {
@@ -496,14 +523,19 @@ __device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R 
   int cur = -1;
   PQ<R> s;
   R pp, px, py, pz, kab;
-  // primitive quartets idx = p, p+P, ... of the ab-major flattened loop
+  // primitive quartets idx = p, p+P, ... of the ab-major flattened loop; the
+  // ket record of the next one is loaded while this one is evaluated
+  KetRec<R> kn;
+  if (p < nprim) load_ket<R>(kp, g, p % g.cd_n, kn);
   for (int idx = p; idx < nprim; idx += P) {
-    const int ip = idx / g.cd_n, iq = idx - ip * g.cd_n;
+    const int ip = idx / g.cd_n;
+    const KetRec<R> kc = kn;
+    if (idx + P < nprim) load_ket<R>(kp, g, (idx + P) % g.cd_n, kn);
     if (ip != cur) {
       load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
       cur = ip;
     }
-    load_prim_cd<R>(kp, g, iq, s, pp, px, py, pz, kab);
+    set_prim_cd<R>(g, kc, s, pp, px, py, pz, kab);
     R u[NR], w[NR];
     rys_roots_all<NR, R>(kp, s.x, u, w);
 #pragma unroll
@@ -558,13 +590,17 @@ __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R
   int cur = -1;
   PQ<R> s;
   R pp, px, py, pz, kab;
+  KetRec<R> kn;
+  if (p < nprim) load_ket<R>(kp, g, p % g.cd_n, kn);
   for (int idx = p; idx < nprim; idx += P) {
-    const int ip = idx / g.cd_n, iq = idx - ip * g.cd_n;
+    const int ip = idx / g.cd_n;
+    const KetRec<R> kc = kn;
+    if (idx + P < nprim) load_ket<R>(kp, g, (idx + P) % g.cd_n, kn);
     if (ip != cur) {
       load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
       cur = ip;
     }
-    load_prim_cd<R>(kp, g, iq, s, pp, px, py, pz, kab);
+    set_prim_cd<R>(g, kc, s, pp, px, py, pz, kab);
     // each root once: lane t evaluates roots t, t+T, ... into the group buffer
     for (int r = t; r < NR; r += T) {
       R uu, ww;
