@@ -54,6 +54,11 @@ HEADLINE = "mixed_df"
 CUTOFF = 1e-12
 FP32_CUTOFF = 1e-2
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) per launch of J/K class kernels of this workload,
+# from one ncu capture each (profiles/ncu_jk_kernels_water8_631gs.md); the
+# roofline's "traffic" when the dominant launch is one of them
+NCU_TRAFFIC = {"jk_kernel<2,0,1,0,fp32,T=1>": 2276352, "jk_kernel<2,0,0,0,dd,T=1>": 585984,
+               "jk_kernel<1,0,0,0,fp32,T=1>": 6786816, "jk_kernel<0,0,0,0,fp32,T=1>": 5455616}
 
 
 def workload(nwater=8, basis="6-31g*", seed=0):
@@ -259,6 +264,8 @@ def run_ours(args):
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(mol, args.cpu_seconds)
+    dom_name = "jk_kernel<%d,%d,%d,%d,%s,T=%d>" % (dom["la"], dom["lb"], dom["lc"], dom["ld"], kind,
+                                                  dom["threads_per_quartet"])
     rec = {
         "metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": ms_hl / steps, "higher_is_better": True, "scaling": "weak",
@@ -283,13 +290,13 @@ def run_ours(args):
         "forces": {"value": world * 1e3 / float(np.mean(t_f[HEADLINE])), "unit": "forces/s",
                    "fp64": world * 1e3 / float(np.mean(t_f["fp64"])),
                    "max_grad_error_mixed_vs_fp64": grad_err, "unit_error": "Eh/bohr",
-                   "note": "derivative integrals: FP32 below the cutoff, FP64 above"},
+                   "note": "derivative integrals: FP32 below the cutoff, double-float above"},
         "autotune_s": tune_s,
         "gpu_launches": (int(st_hl["launches"]) * 3 + int(st_64["launches"])) * steps,
         "roofline": {"bound": pipe, "achieved": achieved, "peak": peaks[pipe], "unit": "TFLOP/s",
-                     "frac": achieved / peaks[pipe] if peaks[pipe] else None, "traffic": None,
-                     "kernel": "jk_kernel<%d,%d,%d,%d,%s,T=%d>" % (dom["la"], dom["lb"], dom["lc"], dom["ld"],
-                                                                   kind, dom["threads_per_quartet"]),
+                     "frac": achieved / peaks[pipe] if peaks[pipe] else None,
+                     "traffic": NCU_TRAFFIC.get(dom_name), "traffic_unit": "bytes per launch (ncu)",
+                     "kernel": dom_name,
                      "kernel_share": dom["ms"] / total_ms if total_ms else None,
                      "peak_source": "live FMA-chain kernel (sf_fma_peak), this run",
                      "build_combined_frac": build_frac},

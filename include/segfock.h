@@ -215,10 +215,9 @@ int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges,
  *   grad[3*A + d] += sum_{pqrs} G_pqrs d(pq|rs)/dR_{A,d},
  *   G_pqrs = 1/2 D_pq D_rs - 1/8 (D_pr D_qs + D_ps D_qr),
  * i.e. the derivative of 1/2 sum_pq D_pq (J - K/2)_pq at fixed D, over the
- * same screened quartets and precision split as sf_fock_jk (the derivative
- * kernels exist in FP64 and FP32: SF_PREC_MIXED_DF runs as SF_PREC_MIXED and
- * SF_PREC_DF as SF_PREC_FP64).  grad (device, 3 doubles per atom index used
- * by the shells) is accumulated, not zeroed. */
+ * same screened quartets and precision split as sf_fock_jk (FP64, FP32 and
+ * double-float derivative kernels).  grad (device, 3 doubles per atom index
+ * used by the shells) is accumulated, not zeroed. */
 int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, double cutoff,
                double fp32_cutoff, void *stream);
 

@@ -903,6 +903,7 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   SF_CK(prepare_md_tc());
   SF_CK(prepare_grad_f64());
   SF_CK(prepare_grad_f32());
+  SF_CK(prepare_grad_dd());
   *out = guard.release();
   g_err.clear();
   return SF_OK;
@@ -1293,27 +1294,19 @@ int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, d
   if (!h) return fail(SF_EINVAL, "sf_grad_jk: NULL handle");
   if (!D || !grad) return fail(SF_EINVAL, "sf_grad_jk: NULL pointer");
   if (precision < SF_PREC_FP64 || precision > SF_PREC_DF) return fail(SF_EINVAL, "sf_grad_jk: bad precision");
-  // the derivative kernels have FP64 and FP32 forms: the double-float modes
-  // take FP64 for their accurate tier
-  if (precision == SF_PREC_MIXED_DF) precision = SF_PREC_MIXED;
-  if (precision == SF_PREC_DF) precision = SF_PREC_FP64;
   if (!(cutoff >= 0.0) || !(fp32_cutoff >= 0.0)) return fail(SF_EINVAL, "sf_grad_jk: bad cutoff");
   if (!h->have_schwarz) return fail(SF_ESTATE, "sf_grad_jk: call sf_schwarz first");
   DeviceGuard g(h->device);
   cudaStream_t st = (cudaStream_t)stream;
   int rc = build_work(h, precision, cutoff, fp32_cutoff);
   if (rc) return rc;
-  const size_t nn = (size_t)h->nao * h->nao;
-  bool need32 = false;
-  for (const auto &s : h->slices) need32 |= s.prec == 1;
-  if (need32) {
-    to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, h->d_D32.p, (int64_t)nn);
-    SF_CK(cudaGetLastError());
-  }
+  rc = convert_density(h, D, h->d_D32.p, st, nullptr);
+  if (rc) return rc;
   auto launch = [&](size_t k, cudaStream_t ss) {
     const auto &s = h->slices[k];
-    return s.prec == 0 ? launch_grad_f64(s.cls, h->kp, s.w, D, grad, ss)
-                       : launch_grad_f32(s.cls, h->kp, s.w, h->d_D32.p, grad, ss);
+    if (s.prec == 0) return launch_grad_f64(s.cls, h->kp, s.w, D, grad, ss);
+    if (s.prec == 1) return launch_grad_f32(s.cls, h->kp, s.w, h->d_D32.p, grad, ss);
+    return launch_grad_dd(s.cls, h->kp, s.w, reinterpret_cast<const dd *>(h->d_Ddd.p), grad, ss);
   };
   if (h->profiling) {   // per-launch events (serialised in mode 2), read by sf_get_slice_info
     while (h->ev.size() < 2 * h->slices.size()) {

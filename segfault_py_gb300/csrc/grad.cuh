@@ -55,8 +55,8 @@ struct GGrp {
 template <typename R>
 __device__ __forceinline__ void load_exps(const KParams &kp, int prim, R &e0, R &e1) {
   const R *rec = prims_of<R>(kp).rec + (size_t)prim * kPrimRec + 6;
-  e0 = __ldg(rec);
-  e1 = __ldg(rec + 1);
+  e0 = ldg_r(rec);
+  e1 = ldg_r(rec + 1);
 }
 
 // T == 1: one lane per quartet, every table in registers, compile-time indices
@@ -198,8 +198,8 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
     ex[k] = 0;
     if (o < Q::NABCD) {
       const int i = a0 + Q::ca(o), j = b0 + Q::cb(o), kk = c0 + Q::cc(o), l = d0 + Q::cd(o);
-      const R Dij = __ldg(D + i * n + j), Dkl = __ldg(D + kk * n + l), Dik = __ldg(D + i * n + kk);
-      const R Djl = __ldg(D + j * n + l), Dil = __ldg(D + i * n + l), Djk = __ldg(D + j * n + kk);
+      const R Dij = ldg_r(D + i * n + j), Dkl = ldg_r(D + kk * n + l), Dik = ldg_r(D + i * n + kk);
+      const R Djl = ldg_r(D + j * n + l), Dil = ldg_r(D + i * n + l), Djk = ldg_r(D + j * n + kk);
       gam[k] = scale * (R)Q::norm(o) * ((R)0.5 * Dij * Dkl - (R)0.125 * (Dik * Djl + Dil * Djk));
       off[k] = G::eoff(o, 0) | (G::eoff(o, 1) << 10) | (G::eoff(o, 2) << 20);
 #pragma unroll
@@ -293,9 +293,9 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
 #pragma unroll
   for (int d = 0; d < 3; ++d)
     for (int sft = 1; sft < TP; sft <<= 1) {
-      gA[d] += __shfl_xor_sync(qmask, gA[d], sft);
-      gB[d] += __shfl_xor_sync(qmask, gB[d], sft);
-      gC[d] += __shfl_xor_sync(qmask, gC[d], sft);
+      gA[d] += shfl_xor_r(qmask, gA[d], sft);
+      gB[d] += shfl_xor_r(qmask, gB[d], sft);
+      gC[d] += shfl_xor_r(qmask, gC[d], sft);
     }
   if (t == 0 && pl == 0) {
     const int at_a = kp.sh.atom[g.a], at_b = kp.sh.atom[g.b], at_c = kp.sh.atom[g.c], at_d = kp.sh.atom[g.d];

@@ -26,7 +26,10 @@ cudaError_t launch_grad_f64(int cls, const KParams &kp, const ClassWork &w, cons
                             cudaStream_t st);
 cudaError_t launch_grad_f32(int cls, const KParams &kp, const ClassWork &w, const float *D, double *grad,
                             cudaStream_t st);
+cudaError_t launch_grad_dd(int cls, const KParams &kp, const ClassWork &w, const dd *D, double *grad,
+                           cudaStream_t st);
 cudaError_t prepare_grad_f64();
+cudaError_t prepare_grad_dd();
 cudaError_t prepare_grad_f32();
 cudaError_t prepare_jk_f64();
 cudaError_t prepare_jk_f32();

@@ -5,7 +5,7 @@ The reference computes energies only.  Here
     dE/dR_A = sum_pq D_pq dH_pq/dR_A - sum_pq W_pq dS_pq/dR_A
               + sum_pqrs G_pqrs d(pq|rs)/dR_A + dE_nuc/dR_A,
     G_pqrs = 1/2 D_pq D_rs - 1/8 (D_pr D_qs + D_ps D_qr),
-    W = 2 sum_occ e_i C_pi C_qi,
+    W = 2 sum_occ e_i C_pi C_qi = (D F D)/2 at the converged density,
 
 with the derivative integrals contracted on the GPU (sf_grad_one_electron,
 sf_grad_jk) and the nuclear term on the host.  ``RHFEnergy`` wraps the SCF
@@ -27,15 +27,12 @@ from .scf import SCFResult, scf_diis
 
 def nuclear_repulsion_gradient(mol: Molecule) -> np.ndarray:
     """d/dR_A of sum_{A<B} Z_A Z_B / |R_A - R_B| (molecule.py:75-80)."""
-    R = mol.xyz__
+    R = np.asarray(mol.xyz__, dtype=np.float64)
     Z = mol.numbers.astype(np.float64)
-    g = np.zeros_like(R)
-    for a in range(mol.natom):
-        for b in range(mol.natom):
-            if a != b:
-                d = R[a] - R[b]
-                g[a] -= Z[a] * Z[b] * d / np.linalg.norm(d) ** 3
-    return g
+    d = R[:, None, :] - R[None, :, :]                  # R_A - R_B
+    r = np.linalg.norm(d, axis=2)
+    np.fill_diagonal(r, np.inf)
+    return -np.einsum("ab,abk->ak", np.outer(Z, Z) / r ** 3, d)
 
 
 def energy_weighted_density(F: torch.Tensor, X: torch.Tensor, norb: int):
@@ -53,11 +50,10 @@ def rhf_gradient(mol: Molecule, res: SCFResult, fb: FockBuilder, precision: str 
     """(natom, 3) gradient in Eh/bohr at the converged SCF ``res``."""
     L = _lib.lib()
     dev = fb.device
-    vals, vecs = torch.linalg.eigh(res.S)
-    X = vecs @ torch.diag(1.0 / torch.sqrt(vals)) @ vecs.T
-    D, W = energy_weighted_density(res.F, X, mol.nelectron // 2)
-    D = D.contiguous()
-    W = W.contiguous()
+    # at the converged SCF: D = 2 C_occ C_occ^T and W = 2 C_occ (C_occ^T F C_occ)
+    # C_occ^T = D F D / 2, orbital-invariant (no diagonalisation needed)
+    D = res.D.contiguous()
+    W = (0.5 * (D @ res.F @ D)).contiguous()
     xyz, Z = mol.atom_table()
     xyz_d = torch.as_tensor(xyz, device=dev)
     Z_d = torch.as_tensor(Z, device=dev)

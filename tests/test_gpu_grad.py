@@ -71,12 +71,30 @@ def test_water_dimer_631gs_gradient_vs_fd(cuda):
         assert abs(fd - g[a, d]) < 1e-6, (a, d, fd, g[a, d])
 
 
-def test_mixed_precision_gradient_error(cuda):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_mixed_precision_gradient_error(cuda, precision):
     from segfault_py_gb300 import geometry as G
     from segfault_py_gb300.molecule import BOHR
     sym, xyz = G.water_cluster(4, seed=2)
     x0 = xyz / BOHR
     e64, g64 = _analytic(sym, x0, "6-31g*")
-    emx, gmx = _analytic(sym, x0, "6-31g*", precision="mixed", fp32_cutoff=1e-2)
+    emx, gmx = _analytic(sym, x0, "6-31g*", precision=precision, fp32_cutoff=1e-2)
     assert abs(emx - e64) < 1e-6
     assert np.abs(gmx - g64).max() < 1e-6
+
+
+def test_double_float_gradient_matches_fp64(cuda):
+    """All-double-float derivative kernels against FP64 at the same converged
+    density: FP64-class agreement (1e-9 Eh/bohr)."""
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.grad import rhf_gradient
+    from segfault_py_gb300.molecule import Molecule
+    from segfault_py_gb300.scf import scf_diis
+    sym, xyz = G.water_cluster(2, seed=3)
+    mol = Molecule.from_geometry(sym, xyz, "6-31g*")
+    fb = FockBuilder(mol, device=cuda)
+    r = scf_diis(mol, tol=1e-10, fb=fb, precision="fp64")
+    g64 = rhf_gradient(mol, r, fb, precision="fp64")
+    gdf = rhf_gradient(mol, r, fb, precision="df")
+    assert float((gdf - g64).abs().max()) < 1e-9
