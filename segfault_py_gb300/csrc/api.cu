@@ -253,6 +253,7 @@ void fill_kparams(sf_handle *h) {
       k.asymdd_w[n][i] = dd(a, b);
     }
   k.nao = h->nao;
+  k.nsm = h->nsm;
   k.natom = h->natom;
   k.err = h->d_err.p;
 }
@@ -787,6 +788,7 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   sf_handle *h = new sf_handle();
   std::unique_ptr<sf_handle> guard(h);
   SF_CK(cudaGetDevice(&h->device));
+  SF_CK(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
   h->nshell = nshell;
   h->spoff.push_back(0);
   int nao = 0;
@@ -893,7 +895,6 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
     SF_CK(cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming));
   }
   SF_CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
-  SF_CK(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
   SF_CK(prepare_jk_f64());
   SF_CK(prepare_jk_f32());
   SF_CK(prepare_jk_dd());

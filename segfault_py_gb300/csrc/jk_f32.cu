@@ -1,4 +1,6 @@
 // jk_f32.cu -- FP32 J/K kernels (FP64 accumulation), one instantiation per class.
+#include <algorithm>
+
 #include "classes.h"
 #include "launch.h"
 
@@ -12,9 +14,13 @@ static cudaError_t run_jk32(const KParams &kp, const ClassWork &w, const float *
   const int P = w.psplit < 1 ? 1 : w.psplit, W = w.wsplit < 1 ? 1 : w.wsplit;
   if (T * P > 32 || (P & (P - 1)) || W > kMaxWsplit) return cudaErrorInvalidValue;
   const int G = kBlock / (T * P);
-  constexpr size_t smem = grp_smem<LA, LB, LC, LD, float, T>();
   auto kern = jk_kernel<LA, LB, LC, LD, float, T>;
-  const int64_t grid = (n * W + G - 1) / G;
+  int64_t grid = (n * W + G - 1) / G;
+  size_t smem = grp_smem<LA, LB, LC, LD, float, T>();
+  if (T == 1) {   // Rys table block in shared memory, grid-stride over the list
+    smem = (size_t)kTabNint * QC<LA, LB, LC, LD>::NR * kTab32Row * sizeof(float);
+    grid = std::min<int64_t>(grid, (int64_t)std::max(kp.nsm, 1) * 16);
+  }
   kern<<<(unsigned)grid, kBlock, smem, st>>>(kp, w, D, Jh, Kh);
   return cudaGetLastError();
 }

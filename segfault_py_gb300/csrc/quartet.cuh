@@ -47,6 +47,7 @@ struct KParams {
   const float4 *tabdd;
   dd asymdd_r[kMaxRoots + 1][kMaxRoots], asymdd_w[kMaxRoots + 1][kMaxRoots];
   int nao;
+  int nsm;             // multiprocessors (grid sizing of the grid-stride kernels)
   int natom;           // atoms referenced by the shells (gradient length / 3)
   int *err;            // device error flag (unused by the arithmetic kernels)
 };
@@ -102,6 +103,10 @@ struct Vec2<double> { using T = double2; };
 template <>
 struct Vec2<float> { using T = float2; };
 
+// FP32 register-path classes with at most this many Cartesian outputs
+// evaluate two primitive quartets per loop iteration (eval_t1_x2)
+constexpr int kX2MaxOutputs = 9;
+
 // FP32: root r at x from its row of (u_k, w_k) pairs, Horner in the row's
 // order k = D .. 0
 __device__ __forceinline__ void rys_row_f32(const float *row, float s, float &u, float &w) {
@@ -115,6 +120,39 @@ __device__ __forceinline__ void rys_row_f32(const float *row, float s, float &u,
     u = u * s + v.x;
     w = w * s + v.y;
   }
+}
+
+// the same from a copy of the n-root block in shared memory
+__device__ __forceinline__ void rys_row_f32_s(const float *row, float s, float &u, float &w) {
+  const float2 *c = reinterpret_cast<const float2 *>(row);
+  const float2 top = c[0];
+  u = top.x;
+  w = top.y;
+#pragma unroll
+  for (int k = 1; k <= kTabDeg32; ++k) {
+    const float2 v = c[k];
+    u = u * s + v.x;
+    w = w * s + v.y;
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void rys_roots_all_f32_s(const KParams &kp, const float *tab_s, float x, float (&u)[N],
+                                                    float (&w)[N]) {
+  if (x >= (float)kTabXmax) {
+    const float ix = 1.0f / x, isx = rsqrtf(x);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      u[i] = kp.asym32.r[N][i] * ix;
+      w[i] = kp.asym32.w[N][i] * isx;
+    }
+    return;
+  }
+  const int j = (int)x;
+  const float s = 2.0f * (x - (float)j) - 1.0f;
+  const float *base = tab_s + j * N * kTab32Row;
+#pragma unroll
+  for (int i = 0; i < N; ++i) rys_row_f32_s(base + i * kTab32Row, s, u[i], w[i]);
 }
 
 template <int N>
@@ -509,14 +547,114 @@ __device__ __forceinline__ double to_f64(float f) { return f2d_alu(f); }
 __device__ __forceinline__ double to_f64(double f) { return f; }
 __device__ __forceinline__ double to_f64(dd f) { return f2d_alu(f.hi) + f2d_alu(f.lo); }
 
+// bra primitive-pair values cached across primitive quartets
+template <typename R>
+struct BraRec {
+  R p, px, py, pz, kab, i2p;
+};
+template <typename R>
+__device__ __forceinline__ void load_bra(const KParams &kp, const QGeom<R> &g, int ip, BraRec<R> &b) {
+  load_rec<R>(prims_of<R>(kp).rec + (size_t)(g.ab_off + ip) * kPrimRec, b.p, b.px, b.py, b.pz, b.kab, b.i2p);
+}
+template <typename R>
+__device__ __forceinline__ void set_pq(const QGeom<R> &g, const BraRec<R> &b, const KetRec<R> &k, PQ<R> &s) {
+  s.i2p = b.i2p;
+  s.pax = b.px - g.Ax; s.pay = b.py - g.Ay; s.paz = b.pz - g.Az;
+  set_prim_cd<R>(g, k, s, b.p, b.px, b.py, b.pz, b.kab);
+}
+
+// all roots, from the shared-memory copy of the FP32 table when given
+template <int N, typename R>
+__device__ __forceinline__ void roots_t1(const KParams &kp, const float *tab_s, R x, R (&u)[N], R (&w)[N]) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (tab_s) {
+      rys_roots_all_f32_s<N>(kp, tab_s, x, u, w);
+      return;
+    }
+  }
+  rys_roots_all<N, R>(kp, x, u, w);
+}
+
+// Rys assembly of one primitive quartet into acc (roots already evaluated)
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void assemble_pq(const QGeom<R> &g, const PQ<R> &s, const R *u, const R *w,
+                                            R (&acc)[QC<LA, LB, LC, LD>::NABCD]) {
+  using Q = QC<LA, LB, LC, LD>;
+  constexpr int NR = Q::NR, SZ = Q::SZ;
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const R uu = u[r];
+    const R b00 = (R)0.5 * s.r2 * uu;
+    const R b10 = s.i2p * ((R)1 - s.aq * uu);
+    const R b01 = s.i2q * ((R)1 - s.ap * uu);
+    const R tq = s.aq * uu, tp = s.ap * uu;
+    R Ix[SZ], Iy[SZ], Iz[SZ];
+    rys_2d<LA, LB, LC, LD, R>((R)1, s.pax - tq * s.pqx, s.qcx + tp * s.pqx, b00, b10, b01, g.ABx, g.CDx, Ix);
+    rys_2d<LA, LB, LC, LD, R>((R)1, s.pay - tq * s.pqy, s.qcy + tp * s.pqy, b00, b10, b01, g.ABy, g.CDy, Iy);
+    rys_2d<LA, LB, LC, LD, R>(s.pref * w[r], s.paz - tq * s.pqz, s.qcz + tp * s.pqz, b00, b10, b01, g.ABz, g.CDz,
+                              Iz);
+#pragma unroll
+    for (int o = 0; o < Q::NABCD; ++o) acc[o] += Ix[Q::toff(o, 0)] * Iy[Q::toff(o, 1)] * Iz[Q::toff(o, 2)];
+  }
+}
+
+// T == 1, FP32, few outputs: two primitive quartets per iteration, their
+// record and table loads issued before either is consumed (the low-L FP32
+// kernels are bound by the latency of these dependent loads); an odd tail
+// repeats the last quartet with a zero prefactor
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void eval_t1_x2(const KParams &kp, const QGeom<R> &g,
+                                           R (&acc)[QC<LA, LB, LC, LD>::NABCD], int p, int P, const float *tab_s) {
+  using Q = QC<LA, LB, LC, LD>;
+  constexpr int NR = Q::NR;
+#pragma unroll
+  for (int o = 0; o < Q::NABCD; ++o) acc[o] = (R)0;
+  const int nprim = g.ab_n * g.cd_n;
+  int cur = -1;
+  BraRec<R> br;
+  for (int idx = p; idx < nprim; idx += 2 * P) {
+    const bool two = idx + P < nprim;
+    const int j2 = two ? idx + P : idx;
+    const int ip1 = idx / g.cd_n, ip2 = j2 / g.cd_n;
+    KetRec<R> k1, k2;
+    load_ket<R>(kp, g, idx - ip1 * g.cd_n, k1);
+    load_ket<R>(kp, g, j2 - ip2 * g.cd_n, k2);
+    if (ip1 != cur) {
+      load_bra<R>(kp, g, ip1, br);
+      cur = ip1;
+    }
+    BraRec<R> b2 = br;
+    if (ip2 != ip1) {
+      load_bra<R>(kp, g, ip2, b2);
+    }
+    PQ<R> s1, s2;
+    set_pq<R>(g, br, k1, s1);
+    set_pq<R>(g, b2, k2, s2);
+    if (!two) s2.pref = (R)0;
+    if (ip2 != ip1) {
+      br = b2;
+      cur = ip2;
+    }
+    R u1[NR], w1[NR], u2[NR], w2[NR];
+    roots_t1<NR, R>(kp, tab_s, s1.x, u1, w1);
+    roots_t1<NR, R>(kp, tab_s, s2.x, u2, w2);
+    assemble_pq<LA, LB, LC, LD, R>(g, s1, u1, w1, acc);
+    assemble_pq<LA, LB, LC, LD, R>(g, s2, u2, w2, acc);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // T == 1: whole quartet in registers; acc[o] unnormalised
 // ---------------------------------------------------------------------------
 template <int LA, int LB, int LC, int LD, typename R>
 __device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R (&acc)[QC<LA, LB, LC, LD>::NABCD],
-                                        int p = 0, int P = 1) {
+                                        int p = 0, int P = 1, const float *tab_s = nullptr) {
   using Q = QC<LA, LB, LC, LD>;
   constexpr int NR = Q::NR, SZ = Q::SZ;
+  if constexpr (std::is_same<R, float>::value && Q::NABCD <= kX2MaxOutputs) {
+    eval_t1_x2<LA, LB, LC, LD, R>(kp, g, acc, p, P, tab_s);
+    return;
+  }
 #pragma unroll
   for (int o = 0; o < Q::NABCD; ++o) acc[o] = (R)0;
   const int nprim = g.ab_n * g.cd_n;
@@ -537,7 +675,7 @@ __device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R 
     }
     set_prim_cd<R>(g, kc, s, pp, px, py, pz, kab);
     R u[NR], w[NR];
-    rys_roots_all<NR, R>(kp, s.x, u, w);
+    roots_t1<NR, R>(kp, tab_s, s.x, u, w);
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
       const R uu = u[r];
@@ -821,6 +959,36 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
   const int P = w.psplit, W = w.wsplit;
   const int TP = T * P;
   const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
+  if constexpr (T == 1 && std::is_same<R, float>::value) {
+    // FP32 register path: the n-root block of the Rys table is copied to
+    // shared memory once per CTA (its rows are read at lane-dependent
+    // intervals: divergent global loads) and the CTA strides over the list
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NR = QC<LA, LB, LC, LD>::NR;
+    constexpr int NTAB4 = kTabNint * NR * kTab32Row / 4;
+    float4 *tab4 = reinterpret_cast<float4 *>(smem_raw);
+    const float4 *src = reinterpret_cast<const float4 *>(kp.tab32 + rys_tab32v_offset(NR));
+    for (int k = threadIdx.x; k < NTAB4; k += blockDim.x) tab4[k] = __ldg(src + k);
+    __syncthreads();
+    const float *tab_s = reinterpret_cast<const float *>(smem_raw);
+    for (int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;; gid += (int64_t)gridDim.x * (kBlock / TP)) {
+      const int64_t q = gid / W;
+      if (q >= w.n) return;
+      const int sub = (int)(gid - q * W) * P + p;
+      const int2 ij = __ldg(w.list + q);
+      const QGeom<R> g = make_geom<R>(kp, w.x0 + ij.x, w.y0 + ij.y, false, false);
+      R scale = (R)1;
+      if (g.a == g.b) scale *= (R)0.5;
+      if (g.c == g.d) scale *= (R)0.5;
+      if (w.same && ij.x == ij.y) scale *= (R)0.5;
+      const int lane = threadIdx.x & 31;
+      const unsigned qmask = (TP == 32) ? 0xffffffffu : (((1u << TP) - 1u) << (lane & ~(TP - 1)));
+      R acc[QC<LA, LB, LC, LD>::NABCD];
+      eval_t1<LA, LB, LC, LD, R>(kp, g, acc, sub, W * P, tab_s);
+      if (P > 1) reduce_psplit<R, QC<LA, LB, LC, LD>::NABCD, 1>(acc, P, qmask);
+      if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh);
+    }
+  }
   const int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;
   const int64_t q = gid / W;
   const int sub = (int)(gid - q * W) * P + p;   // primitive sub-group of the W*P
