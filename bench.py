@@ -28,6 +28,8 @@ Reported:
 * secondary    (H2O)16 6-31G*: mixed vs FP64 Fock builds/s and forces/s
 * eri_batch    1e6 random shell quartets over all 21 classes: raw-ERI
                quartets/s in FP64 and FP32 through one prepared plan
+* alkane       C20H42 6-31G** (510 AOs): graph-captured mixed SCF wall time
+               and errors against FP64, Fock builds/s and forces/s
 
 ``--impl reference`` times the reference's CPU algorithm (oracle port, all host
 cores) on the same workload and prints the same metric.
@@ -258,6 +260,7 @@ def run_ours(args):
     secondary = None
     if args.nwater2 > 0:
         secondary = secondary_config(args.nwater2, basis, max(5, args.steps // 2), args.warmup, flush, dev)
+    alkane = alkane_config(dev, flush, args.warmup) if args.alkane else None
     eri = None
     if args.eri_quartets > 0:
         eri = eri_batch_config(args.eri_quartets, 3, args.warmup, flush, dev, peaks)
@@ -304,6 +307,7 @@ def run_ours(args):
         "clocks": clocks,
         "secondary": secondary,
         "eri_batch": eri,
+        "alkane": alkane,
     }
     print(json.dumps(rec))
     if world > 1:
@@ -350,6 +354,52 @@ def secondary_config(nwater, basis, steps, warmup, flush, dev):
            "energy_error_mixed_fp32_fp64_vs_fp64": e["mixed"] - e["fp64"],
            "max_grad_error_mixed_vs_fp64": gerr,
            "scf_energy_fp64": r.energy}
+    fb.close()
+    return out
+
+
+def alkane_config(dev, flush, warmup):
+    """C20H42 all-trans, 6-31G** (510 AOs): the full mixed-precision SCF
+    captured as one CUDA graph per iteration, plus forces, against the
+    all-FP64 GPU path (energy and gradient errors), and Fock builds/s of both."""
+    import torch
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.grad import rhf_gradient
+    from segfault_py_gb300.molecule import Molecule
+    from segfault_py_gb300.scf import scf_diis
+    from segfault_py_gb300.scf_graph import GraphSCF
+    sym, xyz = G.alkane(20, seed=0)
+    mol = Molecule.from_geometry(sym, xyz, "6-31g**")
+    fb = FockBuilder(mol, device=dev, cutoff=CUTOFF, fp32_cutoff=FP32_CUTOFF, precision=HEADLINE)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    ref = scf_diis(mol, tol=1e-9, dtol=1e-7, fb=fb, precision="fp64")
+    torch.cuda.synchronize()
+    t_ref = time.time() - t0
+    fb.autotune(ref.D.contiguous(), precision=HEADLINE, reps=2)
+    g = GraphSCF(mol, fb=fb, precision=HEADLINE, fp32_cutoff=FP32_CUTOFF).capture()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    r = g.run(tol=1e-9)
+    torch.cuda.synchronize()
+    t_graph = time.time() - t0
+    stream = torch.cuda.current_stream()
+    D = ref.D.contiguous()
+    J, K = torch.empty_like(D), torch.empty_like(D)
+    t = {p: time_steps(lambda: fb.jk(D, precision=p, out=(J, K)), 3, warmup, flush, stream) for p in (HEADLINE, "fp64")}
+    tf = {p: time_steps(lambda: rhf_gradient(mol, ref, fb, precision=p), 3, 1, flush, stream) for p in (HEADLINE, "fp64")}
+    g64 = rhf_gradient(mol, ref, fb, precision="fp64")
+    gmx = rhf_gradient(mol, ref, fb, precision=HEADLINE)
+    out = {"workload": "C20H42 all-trans, 6-31G**, seed 0", "nao": mol.nao,
+           "scf_graph_mixed_s": t_graph, "scf_graph_iterations": r.iterations, "scf_graph_converged": r.converged,
+           "scf_fp64_eager_s": t_ref, "energy_error_mixed_vs_fp64": r.energy - ref.energy,
+           "fock_builds_per_s_mixed": 1e3 / float(np.mean(t[HEADLINE])),
+           "fock_builds_per_s_fp64": 1e3 / float(np.mean(t["fp64"])),
+           "forces_per_s_mixed": 1e3 / float(np.mean(tf[HEADLINE])),
+           "forces_per_s_fp64": 1e3 / float(np.mean(tf["fp64"])),
+           "max_grad_error_mixed_vs_fp64": float((gmx - g64).abs().max()),
+           "scf_energy_fp64": ref.energy}
     fb.close()
     return out
 
@@ -469,6 +519,7 @@ def main():
     ap.add_argument("--nwater2", type=int, default=16, help="second cluster size reported beside (0: off)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--eri-quartets", type=int, default=1_000_000, help="raw-ERI stress batch size (0: off)")
+    ap.add_argument("--no-alkane", dest="alkane", action="store_false", help="skip the C20H42 6-31G** block")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

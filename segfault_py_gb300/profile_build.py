@@ -1,4 +1,4 @@
-"""Per-launch device times of one Fock build.
+"""Per-launch device times of one Fock build (or two-electron gradient).
 
     python -m segfault_py_gb300.profile_build --nwater 8 --precision mixed --fp32-cutoff 1e-2
 
@@ -56,6 +56,8 @@ def main(argv=None):
     ap.add_argument("--slices", action="store_true")
     ap.add_argument("--time", action="store_true", help="also time --builds normal (concurrent) builds with events")
     ap.add_argument("--autotune", action="store_true", help="autotune the launch shapes first")
+    ap.add_argument("--grad", action="store_true",
+                    help="profile the two-electron gradient (sf_grad_jk) instead of the Fock build")
     a = ap.parse_args(argv)
     preload_torch_linalg()
     sym, xyz = geometry.water_cluster(a.nwater)
@@ -68,15 +70,24 @@ def main(argv=None):
         print("autotuned %d launches, serialised time saved %.4f ms" % (len(tab), gain))
     if a.slices:
         fb.set_profiling(2)
-    for _ in range(a.builds):
-        fb.jk(D, stats=True)
+    if a.grad:
+        from . import _lib
+        from .fock import _ptr, _stream_ptr
+        fb.jk(D, stats=True)   # work counters; the slice times below are the gradient's
+        g = torch.zeros(3 * mol.natom, dtype=torch.float64, device=fb.device)
+        for _ in range(a.builds):
+            _lib.check(_lib.lib().sf_grad_jk(fb.handle, _ptr(D), _ptr(g), _lib.PRECISION[a.precision], a.cutoff,
+                                             a.fp32_cutoff, _stream_ptr()))
+    else:
+        for _ in range(a.builds):
+            fb.jk(D, stats=True)
     torch.cuda.synchronize()
     print("== %s nao=%d builds=%d stats %s" % (a.precision, fb.nao, a.builds, json.dumps(fb.last_stats)))
     if a.slices:
         tot, rows = slice_table(fb)
         print("serialised kernel time of one build: %.4f ms" % tot)
         print("\n".join(rows))
-    if a.time:
+    if a.time and not a.grad:
         fb.set_profiling(0)
         J = torch.empty_like(D)
         K = torch.empty_like(D)
