@@ -299,12 +299,23 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
     }
   if (t == 0 && pl == 0) {
     const int at_a = kp.sh.atom[g.a], at_b = kp.sh.atom[g.b], at_c = kp.sh.atom[g.c], at_d = kp.sh.atom[g.d];
+    R gD[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      atomicAdd(grad + 3 * at_a + d, to_f64(gA[d]));
-      atomicAdd(grad + 3 * at_b + d, to_f64(gB[d]));
+      gD[d] = -(gA[d] + gB[d] + gC[d]);
       atomicAdd(grad + 3 * at_c + d, to_f64(gC[d]));
-      atomicAdd(grad + 3 * at_d + d, -to_f64(gA[d] + gB[d] + gC[d]));
+      atomicAdd(grad + 3 * at_d + d, to_f64(gD[d]));
+    }
+    // centres a, b: with one quartet per lane, the lanes sharing the bra pair
+    // (consecutive in the cost-sorted list) add their forces first
+    R gab[6] = {gA[0], gA[1], gA[2], gB[0], gB[1], gB[2]};
+    const bool write = TP > 1 ? true : run_sums<R, 6>(ij.x, gab);
+    if (write) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        atomicAdd(grad + 3 * at_a + d, to_f64(gab[d]));
+        atomicAdd(grad + 3 * at_b + d, to_f64(gab[3 + d]));
+      }
     }
   }
 }

@@ -68,6 +68,34 @@ __device__ __forceinline__ dd ldg_r(const dd *p) { return dd_ldg(p); }
 __device__ __forceinline__ float shfl_xor_r(unsigned m, float v, int k) { return __shfl_xor_sync(m, v, k); }
 __device__ __forceinline__ double shfl_xor_r(unsigned m, double v, int k) { return __shfl_xor_sync(m, v, k); }
 __device__ __forceinline__ dd shfl_xor_r(unsigned m, dd v, int k) { return dd_shfl_xor(m, v, k); }
+__device__ __forceinline__ float shfl_up_r(unsigned m, float v, int k) { return __shfl_up_sync(m, v, k); }
+__device__ __forceinline__ double shfl_up_r(unsigned m, double v, int k) { return __shfl_up_sync(m, v, k); }
+__device__ __forceinline__ dd shfl_up_r(unsigned m, dd v, int k) {
+  return dd(__shfl_up_sync(m, v.hi, k), __shfl_up_sync(m, v.lo, k));
+}
+
+// Sums of v[0..N) over runs of equal key among the active lanes of a warp
+// (runs must be contiguous: consecutive quartets of a cost-sorted list share
+// their bra pair): segmented inclusive scan by shuffles; returns true on the
+// last lane of its run, which then holds the run's sums.  Lets one atomic per
+// run replace one per lane on addresses all lanes of the run share.
+template <typename R, int N>
+__device__ __forceinline__ bool run_sums(int key, R (&v)[N]) {
+  const unsigned mask = __activemask();
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int k = __shfl_up_sync(mask, key, off);
+    const bool take = lane >= off && ((mask >> (lane - off)) & 1u) && k == key;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const R o = shfl_up_r(mask, v[i], off);
+      if (take) v[i] += o;
+    }
+  }
+  const int kn = __shfl_down_sync(mask, key, 1);
+  return lane == 31 || !((mask >> (lane + 1)) & 1u) || kn != key;
+}
 
 // 1/sqrt(a): single-precision hardware seed + two Newton-Raphson steps
 // y <- y (3/2 - a/2 y^2) (quadratic convergence: 2^-23 -> 2^-46 -> rounding).
@@ -795,14 +823,16 @@ __device__ __forceinline__ void reduce_psplit(R (&acc)[N], int P, unsigned qmask
 // ---------------------------------------------------------------------------
 template <int LA, int LB, int LC, int LD, typename R>
 __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, const R (&acc)[QC<LA, LB, LC, LD>::NABCD],
-                                          R scale, const R *__restrict__ D, double *Jh, double *Kh) {
+                                          R scale, const R *__restrict__ D, double *Jh, double *Kh, int bra_key = -1) {
   using Q = QC<LA, LB, LC, LD>;
   const int n = kp.nao;
   const int a0 = kp.sh.ao[g.a], b0 = kp.sh.ao[g.b], c0 = kp.sh.ao[g.c], d0 = kp.sh.ao[g.d];
   R v[Q::NABCD];
 #pragma unroll
   for (int o = 0; o < Q::NABCD; ++o) v[o] = acc[o] * (R)Q::norm(o);
-  // J_ab and K blocks need D of the other pairs
+  // J_ab and K blocks need D of the other pairs.  J_ab: with one quartet per
+  // lane (bra_key >= 0) the lanes sharing the bra pair add their J_ab first
+  R sj[Q::NA * Q::NB];
 #pragma unroll
   for (int ia = 0; ia < Q::NA; ++ia)
 #pragma unroll
@@ -813,8 +843,15 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
 #pragma unroll
         for (int id = 0; id < Q::ND; ++id)
           s += v[((ia * Q::NB + ib) * Q::NC + ic) * Q::ND + id] * ldg_r(D + (c0 + ic) * n + d0 + id);
-      atomicAdd(Jh + (a0 + ia) * n + b0 + ib, to_f64((R)2 * scale * s));
+      sj[ia * Q::NB + ib] = (R)2 * scale * s;
     }
+  const bool write_j = bra_key < 0 ? true : run_sums<R, Q::NA * Q::NB>(bra_key, sj);
+  if (write_j) {
+#pragma unroll
+    for (int ia = 0; ia < Q::NA; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < Q::NB; ++ib) atomicAdd(Jh + (a0 + ia) * n + b0 + ib, to_f64(sj[ia * Q::NB + ib]));
+  }
 #pragma unroll
   for (int ic = 0; ic < Q::NC; ++ic)
 #pragma unroll
@@ -986,7 +1023,7 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
       R acc[QC<LA, LB, LC, LD>::NABCD];
       eval_t1<LA, LB, LC, LD, R>(kp, g, acc, sub, W * P, tab_s);
       if (P > 1) reduce_psplit<R, QC<LA, LB, LC, LD>::NABCD, 1>(acc, P, qmask);
-      if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh);
+      if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh, P == 1 ? ij.x : -1);
     }
   }
   const int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;
@@ -1007,7 +1044,7 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
     R acc[QC<LA, LB, LC, LD>::NABCD];
     eval_t1<LA, LB, LC, LD, R>(kp, g, acc, sub, W * P);
     if (P > 1) reduce_psplit<R, QC<LA, LB, LC, LD>::NABCD, 1>(acc, P, qmask);
-    if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh);
+    if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh, P == 1 ? i : -1);
   } else {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using GP = Grp<LA, LB, LC, LD, R, T>;
