@@ -1353,6 +1353,8 @@ int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *cha
   P.charges = charges;
   P.natom = natom;
   P.S = P.T = P.V = nullptr;
+  P.tab64 = h->kp.tab64;
+  P.asym = h->kp.asym;
   SF_CK(launch_one_electron_grad(P, D, W, grad, (cudaStream_t)stream));
   return SF_OK;
 }
@@ -1468,6 +1470,8 @@ int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges,
   P.S = S;
   P.T = T;
   P.V = V;
+  P.tab64 = h->kp.tab64;
+  P.asym = h->kp.asym;
   SF_CK(launch_one_electron(P, (cudaStream_t)stream));
   return SF_OK;
 }

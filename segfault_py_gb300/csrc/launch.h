@@ -46,6 +46,8 @@ struct OneParams {
   const double *atom_xyz, *charges;
   int natom;
   double *S, *T, *V;
+  const double *tab64;          // FP64 Rys rule (Boys values of the gradient kernel)
+  RysAsym asym;
 };
 
 cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st);

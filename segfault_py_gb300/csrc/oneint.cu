@@ -19,8 +19,6 @@
 
 namespace sf {
 
-constexpr int kOneMaxL = 2;
-constexpr int kOneMaxN = 2 * kOneMaxL;      // Boys orders needed by V
 
 // F_n(T) for n = 0..nmax (nmax <= 8)
 __device__ void boys_array(int nmax, double T, double *F) {
@@ -77,7 +75,6 @@ __device__ void one_pair(const OneParams &P, int a, int b) {
   constexpr int NA = ncart(LA), NB = ncart(LB);
   const double A[3] = {P.sh.cx[a], P.sh.cy[a], P.sh.cz[a]};
   const double B[3] = {P.sh.cx[b], P.sh.cy[b], P.sh.cz[b]};
-  const double AB2 = (A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) + (A[2] - B[2]) * (A[2] - B[2]);
   double s[NA][NB], k[NA][NB], v[NA][NB];
 #pragma unroll
   for (int i = 0; i < NA; ++i)
@@ -202,33 +199,37 @@ cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------
 // Gradient of E1 = sum_ij D_ij (T_ij + V_ij) - W_ij S_ij.  With D, W and the
-// operators symmetric, d/dR sum_ij D_ij O_ij = 2 sum_ij D_ij <d phi_i/dR|O|phi_j>,
-// so only the bra function of each ordered shell pair is differentiated,
-// d phi_a / dA = 2 alpha phi_{a+1} - a phi_{a-1}, and counted twice.
-// ---------------------------------------------------------------------------
-// CTA per ordered shell pair (a, b), 64 threads.  For every primitive pair:
-//  * E coefficients (bra shifted to LA+1, ket to LB+2) into shared memory;
-//  * S and T bra-derivative terms (nucleus independent) by thread 0;
-//  * the density-contracted Hermite coefficients of the bra derivative,
-//      M^d_tuv = 2pi/p c_i c_j sum_{i in a, j in b} D_ij sum_+- f E^{i+-1_d, j}_t E_u E_v,
-//    cooperatively into shared memory (they do not depend on the nucleus);
-//  * every thread then takes nuclei C = t, t+64, ...: R_tuv(p, P - C) by the
-//    Hermite Coulomb recursion and dV/dA_d = -Z_C sum_tuv M^d_tuv R_tuv.
-// Each ordered pair counts twice (bra derivative of (a,b) = ket derivative of
-// (b,a)); the nucleus receives minus the basis-centre part (translational
-// invariance of <a|1/r_C|b>).
+// operators symmetric, d/dR sum_ij D_ij O_ij = 2 sum_ij D_ij <d phi_i/dR|O|phi_j>
+// over ordered shell pairs; per canonical pair (a >= b) both the bra and the
+// ket derivative are taken, d phi/dA = 2 alpha phi_{+1} - a phi_{-1}:
+//  * S and T (two-centre): the ket derivative is minus the bra one;
+//  * V: the bra and ket derivative share R_tuv(p, P - C) of each nucleus C,
+//    which receives minus their sum (translational invariance of
+//    <a|1/r_C|b>).
+// CTA per canonical pair (a, b), 64 threads.  For every primitive pair:
+//  * E coefficients (bra to LA+1, ket to LB+2) into shared memory;
+//  * the S and T bra-derivative terms by thread 0;
+//  * the density-contracted Hermite coefficients of the bra and the ket
+//    derivative, M^d_tuv = 2pi/p c_i c_j sum_{i in a, j in b} D_ij sum_+- f
+//    E.. E.. E.. (nucleus independent), cooperatively into shared memory;
+//  * every thread takes nuclei C = t, t+64, ...: Boys values F_m(p |P-C|^2)
+//    = sum_i w_i u_i^m from the FP64 Rys rule of floor(L/2)+1 points (exact
+//    for m <= L), R_tuv by the Hermite Coulomb recursion, and
+//    dV/dX_d = -Z_C sum_tuv M^d_tuv R_tuv.
 constexpr int kOneGradThreads = 64;
 
 template <int LA, int LB>
 __device__ void one_pair_grad2(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b) {
   constexpr int NA = ncart(LA), NB = ncart(LB);
   constexpr int LE = LA + 1, L = LA + LB + 1, NH = (L + 1) * (L + 1) * (L + 1);
+  constexpr int NRT = L / 2 + 1;   // Rys points whose rule is exact for F_0 .. F_L
   const double pi = 3.14159265358979323846;
   __shared__ double E[3][LE + 1][LB + 3][LE + LB + 3];
-  __shared__ double M[3][NH];
+  __shared__ double MA[3][NH], MB[3][NH];
   __shared__ double Dab[NA][NB];
-  __shared__ double red[kOneGradThreads][3];
+  __shared__ double red[kOneGradThreads][6];
   const int tid = threadIdx.x;
+  const bool two = a != b;   // canonical pair with a distinct ket: ket derivative too
   const double A[3] = {P.sh.cx[a], P.sh.cy[a], P.sh.cz[a]};
   const double B[3] = {P.sh.cx[b], P.sh.cy[b], P.sh.cz[b]};
   const int a0 = P.sh.ao[a], b0 = P.sh.ao[b], n = P.nao;
@@ -236,7 +237,7 @@ __device__ void one_pair_grad2(const OneParams &P, const double *Dm, const doubl
     const int i = k / NB, j = k % NB;
     Dab[i][j] = Dm[(a0 + i) * n + b0 + j] * cart_norm(LA, i) * cart_norm(LB, j);
   }
-  double gA[3] = {0.0, 0.0, 0.0};
+  double gST[3] = {0.0, 0.0, 0.0}, gVA[3] = {0.0, 0.0, 0.0}, gVB[3] = {0.0, 0.0, 0.0};
   for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
     for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
       const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
@@ -282,41 +283,75 @@ __device__ void one_pair_grad2(const OneParams &P, const double *Dm, const doubl
                 dS += f * s0;
                 dT += f * t;
               }
-              gA[d] += cc * (Dij * dT - Wij * dS);
+              gST[d] += cc * (Dij * dT - Wij * dS);
             }
           }
       }
-      // density-contracted Hermite coefficients of the bra derivative
+      // density-contracted Hermite coefficients of the bra (MA) and ket (MB) derivatives
       const double pre = 2.0 * pi / p * cc;
       for (int k = tid; k < 3 * NH; k += blockDim.x) {
         const int d = k / NH, h = k % NH;
         const int t = h / ((L + 1) * (L + 1)), u = (h / (L + 1)) % (L + 1), v = h % (L + 1);
-        double m = 0.0;
+        double ma = 0.0, mb = 0.0;
         if (t + u + v <= L) {
           for (int i = 0; i < NA; ++i)
             for (int j = 0; j < NB; ++j) {
-              const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
-              double acc = 0.0;
+              const int ax0[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
+              const int bx0[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
+              double acca = 0.0, accb = 0.0;
               for (int sgn = 0; sgn < 2; ++sgn) {
-                int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
-                const int ad = ax[d];
-                if (sgn == 1 && ad == 0) continue;
-                ax[d] += sgn == 0 ? 1 : -1;
-                if (t > ax[0] + bx[0] || u > ax[1] + bx[1] || v > ax[2] + bx[2]) continue;
-                const double f = sgn == 0 ? 2.0 * al : -(double)ad;
-                acc += f * E[0][ax[0]][bx[0]][t] * E[1][ax[1]][bx[1]][u] * E[2][ax[2]][bx[2]][v];
+                {
+                  int ax[3] = {ax0[0], ax0[1], ax0[2]};
+                  const int ad = ax[d];
+                  if (!(sgn == 1 && ad == 0)) {
+                    ax[d] += sgn == 0 ? 1 : -1;
+                    if (t <= ax[0] + bx0[0] && u <= ax[1] + bx0[1] && v <= ax[2] + bx0[2]) {
+                      const double f = sgn == 0 ? 2.0 * al : -(double)ad;
+                      acca += f * E[0][ax[0]][bx0[0]][t] * E[1][ax[1]][bx0[1]][u] * E[2][ax[2]][bx0[2]][v];
+                    }
+                  }
+                }
+                if (two) {
+                  int bx[3] = {bx0[0], bx0[1], bx0[2]};
+                  const int bd = bx[d];
+                  if (!(sgn == 1 && bd == 0)) {
+                    bx[d] += sgn == 0 ? 1 : -1;
+                    if (t <= ax0[0] + bx[0] && u <= ax0[1] + bx[1] && v <= ax0[2] + bx[2]) {
+                      const double f = sgn == 0 ? 2.0 * be : -(double)bd;
+                      accb += f * E[0][ax0[0]][bx[0]][t] * E[1][ax0[1]][bx[1]][u] * E[2][ax0[2]][bx[2]][v];
+                    }
+                  }
+                }
               }
-              m += Dab[i][j] * acc;
+              ma += Dab[i][j] * acca;
+              mb += Dab[i][j] * accb;
             }
         }
-        M[d][h] = pre * m;
+        MA[d][h] = pre * ma;
+        MB[d][h] = pre * mb;
       }
       __syncthreads();
       for (int at = tid; at < P.natom; at += blockDim.x) {
         const double pc[3] = {Pc[0] - P.atom_xyz[3 * at], Pc[1] - P.atom_xyz[3 * at + 1],
                               Pc[2] - P.atom_xyz[3 * at + 2]};
         double F[L + 1];
-        boys_array(L, p * (pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]), F);
+        {
+          double ur[NRT], wr[NRT];
+          rys_roots_f64_tab<NRT>(P.tab64, P.asym, p * (pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]), ur, wr);
+          double pw[NRT];
+#pragma unroll
+          for (int r = 0; r < NRT; ++r) pw[r] = wr[r];
+#pragma unroll
+          for (int m = 0; m <= L; ++m) {
+            double f = 0.0;
+#pragma unroll
+            for (int r = 0; r < NRT; ++r) {
+              f += pw[r];
+              pw[r] *= ur[r];
+            }
+            F[m] = f;
+          }
+        }
         double R[L + 1][L + 1][L + 1][L + 1];
         for (int m = 0; m <= L; ++m) {
           double f = F[m];
@@ -334,36 +369,45 @@ __device__ void one_pair_grad2(const OneParams &P, const double *Dm, const doubl
                 else r = (w > 1 ? (w - 1) * R[m + 1][t][u][w - 2] : 0.0) + pc[2] * R[m + 1][t][u][w - 1];
                 R[m][t][u][w] = r;
               }
-        double dv[3] = {0.0, 0.0, 0.0};
+        double da[3] = {0.0, 0.0, 0.0}, db[3] = {0.0, 0.0, 0.0};
         for (int t = 0; t <= L; ++t)
           for (int u = 0; u <= L - t; ++u)
             for (int w = 0; w <= L - t - u; ++w) {
               const int h = (t * (L + 1) + u) * (L + 1) + w;
               const double rr = R[0][t][u][w];
-              dv[0] += M[0][h] * rr;
-              dv[1] += M[1][h] * rr;
-              dv[2] += M[2][h] * rr;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+                da[d] += MA[d][h] * rr;
+                db[d] += MB[d][h] * rr;
+              }
             }
         const double z = -P.charges[at];
         for (int d = 0; d < 3; ++d) {
-          gA[d] += z * dv[d];
-          atomicAdd(grad + 3 * at + d, -2.0 * z * dv[d]);
+          gVA[d] += z * da[d];
+          gVB[d] += z * db[d];
+          atomicAdd(grad + 3 * at + d, -2.0 * z * (da[d] + db[d]));
         }
       }
     }
-  // reduce gA over the CTA, one atomic per direction
-  for (int d = 0; d < 3; ++d) red[tid][d] = gA[d];
+  // reduce over the CTA, one atomic per centre and direction
+  for (int d = 0; d < 3; ++d) {
+    red[tid][d] = gVA[d] + gST[d];
+    red[tid][3 + d] = gVB[d] - gST[d];
+  }
   __syncthreads();
-  if (tid < 3) {
+  if (tid < 6) {
     double sacc = 0.0;
     for (int k = 0; k < (int)blockDim.x; ++k) sacc += red[k][tid];
-    atomicAdd(grad + 3 * P.sh.atom[a] + tid, 2.0 * sacc);
+    if (tid < 3) atomicAdd(grad + 3 * P.sh.atom[a] + tid, 2.0 * sacc);
+    else if (two) atomicAdd(grad + 3 * P.sh.atom[b] + tid - 3, 2.0 * sacc);
   }
 }
 
+// one CTA per ordered (a, b) index of the grid; the canonical ones (a >= b) work
 __global__ void __launch_bounds__(kOneGradThreads) one_electron_grad_kernel(OneParams P, const double *D,
                                                                             const double *W, double *grad) {
   const int a = blockIdx.x / P.nshell, b = blockIdx.x % P.nshell;
+  if (b > a) return;
   switch (P.sh.l[a] * 3 + P.sh.l[b]) {
     case 0: one_pair_grad2<0, 0>(P, D, W, grad, a, b); break;
     case 1: one_pair_grad2<0, 1>(P, D, W, grad, a, b); break;

@@ -263,15 +263,18 @@ __device__ __forceinline__ void rys_roots_all(const KParams &kp, R x, R (&u)[N],
   }
 }
 
+// the FP64 rule from an explicit table and asymptotic constants (also used by
+// the one-electron kernels, whose Boys values are sum_i w_i u_i^m)
 template <int N>
-__device__ __forceinline__ void rys_roots_all_f64(const KParams &kp, double x, double (&u)[N], double (&w)[N]) {
+__device__ __forceinline__ void rys_roots_f64_tab(const double *tab64, const RysAsym &asym, double x,
+                                                  double (&u)[N], double (&w)[N]) {
   using R = double;
   if (x >= (R)kTabXmax) {
     const R ix = (R)1 / x, isx = rsqrt_nr(x);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      u[i] = (R)kp.asym.r[N][i] * ix;
-      w[i] = (R)kp.asym.w[N][i] * isx;
+      u[i] = (R)asym.r[N][i] * ix;
+      w[i] = (R)asym.w[N][i] * isx;
     }
     return;
   }
@@ -279,7 +282,7 @@ __device__ __forceinline__ void rys_roots_all_f64(const KParams &kp, double x, d
   constexpr int D = TabDeg<R>::v;
   const int j = (int)x;
   const R s = (R)2 * (x - (R)j) - (R)1;
-  const V *c = reinterpret_cast<const V *>(tab_of<R>(kp) + rys_tab_offset(N, D) + j * (D + 1) * 2 * N);
+  const V *c = reinterpret_cast<const V *>(tab64 + rys_tab_offset(N, D) + j * (D + 1) * 2 * N);
   R f[2 * N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
@@ -301,6 +304,11 @@ __device__ __forceinline__ void rys_roots_all_f64(const KParams &kp, double x, d
     u[i] = f[i];
     w[i] = f[N + i];
   }
+}
+
+template <int N>
+__device__ __forceinline__ void rys_roots_all_f64(const KParams &kp, double x, double (&u)[N], double (&w)[N]) {
+  rys_roots_f64_tab<N>(kp.tab64, kp.asym, x, u, w);
 }
 
 // one root r of the n-point rule
