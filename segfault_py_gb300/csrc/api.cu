@@ -210,6 +210,7 @@ struct sf_handle {
   // add into Jh/Kh with atomics), so they are spread over kSideStreams
   // streams forked from and joined back into the caller's stream
   static constexpr int kSideStreams = 16;
+  static constexpr int kHiStreams = 6;   // high-priority side streams (accurate tier of a mixed build)
   cudaStream_t side[kSideStreams] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[kSideStreams] = {};
   std::vector<int> slice_stream;   // side stream of each slice (greedy by cost)
@@ -278,12 +279,13 @@ int64_t count_pass(const double *qy, int ny, double qi, double cut) {
 
 // greedy longest-processing-time assignment of jobs (cost descending) to
 // the side streams
-std::vector<int> lpt_streams(const std::vector<double> &cost_desc) {
+std::vector<int> lpt_streams(const std::vector<double> &cost_desc, int first = 0,
+                             int last = sf_handle::kSideStreams) {
   double load[sf_handle::kSideStreams] = {0};
-  std::vector<int> s(cost_desc.size(), 0);
+  std::vector<int> s(cost_desc.size(), first);
   for (size_t k = 0; k < cost_desc.size(); ++k) {
-    int best = 0;
-    for (int j = 1; j < sf_handle::kSideStreams; ++j)
+    int best = first;
+    for (int j = first + 1; j < last; ++j)
       if (load[j] < load[best]) best = j;
     s[k] = best;
     load[best] += cost_desc[k];
@@ -493,7 +495,22 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     for (int k : order) sorted.push_back(h->slices[k]);
     h->slices.swap(sorted);
     std::sort(cost.begin(), cost.end(), std::greater<double>());
-    h->slice_stream = lpt_streams(cost);
+    bool has32 = false, hasacc = false;
+    for (const auto &sl : h->slices) (sl.prec == 1 ? has32 : hasacc) = true;
+    if (has32 && hasacc) {
+      // mixed build: accurate-tier launches on the high-priority streams,
+      // FP32 launches on the others, each group balanced by LPT
+      std::vector<double> ca, cf;
+      for (size_t k = 0; k < h->slices.size(); ++k) (h->slices[k].prec == 1 ? cf : ca).push_back(cost[k]);
+      const std::vector<int> sa = lpt_streams(ca, 0, sf_handle::kHiStreams);
+      const std::vector<int> sf = lpt_streams(cf, sf_handle::kHiStreams, sf_handle::kSideStreams);
+      h->slice_stream.assign(h->slices.size(), 0);
+      size_t ia = 0, ifp = 0;
+      for (size_t k = 0; k < h->slices.size(); ++k)
+        h->slice_stream[k] = h->slices[k].prec == 1 ? sf[ifp++] : sa[ia++];
+    } else {
+      h->slice_stream = lpt_streams(cost);
+    }
   }
   h->c_prec = prec;
   h->c_cut = cut;
@@ -890,9 +907,17 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   SF_CK(cudaMemset(h->d_err.p, 0, 4 * sizeof(int)));
   int rc = upload_pairs(h);
   if (rc) return rc;
-  for (int k = 0; k < sf_handle::kSideStreams; ++k) {
-    SF_CK(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking));
-    SF_CK(cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming));
+  {
+    // the first kHiStreams side streams run at the device's highest priority:
+    // in the mixed modes they carry the accurate tier's few, long-running
+    // CTAs, which then start as soon as an SM frees up instead of queueing
+    // behind the FP32 launches
+    int lo = 0, hi = 0;
+    SF_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    for (int k = 0; k < sf_handle::kSideStreams; ++k) {
+      SF_CK(cudaStreamCreateWithPriority(&h->side[k], cudaStreamNonBlocking, k < sf_handle::kHiStreams ? hi : lo));
+      SF_CK(cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming));
+    }
   }
   SF_CK(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
   SF_CK(prepare_jk_f64());
