@@ -186,6 +186,7 @@ struct sf_handle {
   DBuf<float> d_ppdd;              // records as (hi, lo) float pairs
   DBuf<float> d_cdd;               // centres x, y, z as dd: 3 blocks of nshell (hi, lo)
   DBuf<float4> d_tabdd;
+  DBuf<float4> d_pair32;           // packed FP32 pair geometry (KParams::pair32)
   DBuf<float> d_Ddd;               // density as dd (per build)
   DBuf<float> d_cx32, d_cy32, d_cz32;
   DBuf<double> d_tab64;
@@ -241,6 +242,7 @@ void fill_kparams(sf_handle *h) {
   k.asym = host_tables().asym;
   k.asym32 = host_tables().asym32;
   k.pdd = DevPrims<dd>{reinterpret_cast<const dd *>(h->d_ppdd.p)};
+  k.pair32 = h->d_pair32.p;
   k.cxd = reinterpret_cast<const dd *>(h->d_cdd.p);
   k.cyd = k.cxd + h->nshell;
   k.czd = k.cyd + h->nshell;
@@ -260,6 +262,21 @@ void fill_kparams(sf_handle *h) {
 }
 
 int upload_pairs(sf_handle *h) {
+  {
+    std::vector<float4> pg(3 * h->pa.size());
+    for (size_t i = 0; i < h->pa.size(); ++i) {
+      const int a = h->pa[i], b = h->pb[i];
+      pg[3 * i] = make_float4((float)h->cx[a], (float)h->cy[a], (float)h->cz[a], (float)(h->cx[a] - h->cx[b]));
+      float ao_a, ao_b, poff, np, fa, fb;
+      const int ia = h->ao[a], ib = h->ao[b], ip = h->ppoff[i], inp = h->pnp[i];
+      std::memcpy(&ao_a, &ia, 4); std::memcpy(&ao_b, &ib, 4);
+      std::memcpy(&poff, &ip, 4); std::memcpy(&np, &inp, 4);
+      std::memcpy(&fa, &a, 4); std::memcpy(&fb, &b, 4);
+      pg[3 * i + 1] = make_float4((float)(h->cy[a] - h->cy[b]), (float)(h->cz[a] - h->cz[b]), ao_a, ao_b);
+      pg[3 * i + 2] = make_float4(poff, np, fa, fb);
+    }
+    SF_CK(h->d_pair32.upload(pg));
+  }
   SF_CK(h->d_pa.upload(h->pa));
   SF_CK(h->d_pb.upload(h->pb));
   SF_CK(h->d_ppoff.upload(h->ppoff));

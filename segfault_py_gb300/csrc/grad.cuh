@@ -187,7 +187,7 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
   // G_o of this lane's outputs (normalised, permutation count folded in),
   // packed table offsets and Cartesian exponents of a, b, c per direction
   const int n = kp.nao;
-  const int a0 = kp.sh.ao[g.a], b0 = kp.sh.ao[g.b], c0 = kp.sh.ao[g.c], d0 = kp.sh.ao[g.d];
+  const int a0 = g.a0, b0 = g.b0, c0 = g.c0, d0 = g.d0;
   R gam[NPER];
   int off[NPER], ex[NPER];
 #pragma unroll

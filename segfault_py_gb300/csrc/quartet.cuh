@@ -43,6 +43,7 @@ struct KParams {
   // double-float copies: primitive-pair records (8 dd), centres, the FP64
   // Rys table as dd rows (rys_tabdd_offset) and the asymptotic constants
   DevPrims<dd> pdd;
+  const float4 *pair32;   // per canonical pair: (Ax,Ay,Az,ABx) (ABy,ABz,ao_a,ao_b) (poff,np,a,b), FP32 / int bits
   const dd *cxd, *cyd, *czd;
   const float4 *tabdd;
   dd asymdd_r[kMaxRoots + 1][kMaxRoots], asymdd_w[kMaxRoots + 1][kMaxRoots];
@@ -446,6 +447,7 @@ __device__ __forceinline__ void rys_2d(R g0, R c00, R c00p, R b00, R b10, R b01,
 template <typename R>
 struct QGeom {
   int a, b, c, d;
+  int a0, b0, c0, d0;                  // first AO of each shell
   int ab_off, ab_n, cd_off, cd_n;
   R Ax, Ay, Az, Cx, Cy, Cz;
   R ABx, ABy, ABz, CDx, CDy, CDz;
@@ -476,6 +478,7 @@ __device__ __forceinline__ QGeom<R> make_geom(const KParams &kp, int pab, int pc
   if (swap_ab) { int t = a; a = b; b = t; }
   if (swap_cd) { int t = c; c = d; d = t; }
   g.a = a; g.b = b; g.c = c; g.d = d;
+  g.a0 = kp.sh.ao[a]; g.b0 = kp.sh.ao[b]; g.c0 = kp.sh.ao[c]; g.d0 = kp.sh.ao[d];
   g.ab_off = kp.pr.poff[pab]; g.ab_n = kp.pr.np[pab];
   g.cd_off = kp.pr.poff[pcd]; g.cd_n = kp.pr.np[pcd];
   const R *X = centre_in<R>(kp, 0), *Y = centre_in<R>(kp, 1), *Z = centre_in<R>(kp, 2);
@@ -483,6 +486,25 @@ __device__ __forceinline__ QGeom<R> make_geom(const KParams &kp, int pab, int pc
   g.Cx = X[c]; g.Cy = Y[c]; g.Cz = Z[c];
   g.ABx = g.Ax - X[b]; g.ABy = g.Ay - Y[b]; g.ABz = g.Az - Z[b];
   g.CDx = g.Cx - X[d]; g.CDy = g.Cy - Y[d]; g.CDz = g.Cz - Z[d];
+  return g;
+}
+
+// FP32 geometry of a quartet from the packed pair records (three 16-byte
+// loads per pair instead of about twenty scattered loads of pair, shell and
+// centre arrays; the quartet set-up is a latency chain in the light classes)
+__device__ __forceinline__ QGeom<float> make_geom32(const KParams &kp, int pab, int pcd) {
+  QGeom<float> g;
+  const float4 *pa = kp.pair32 + 3 * (size_t)pab, *pc = kp.pair32 + 3 * (size_t)pcd;
+  const float4 a0 = __ldg(pa), a1 = __ldg(pa + 1), a2 = __ldg(pa + 2);
+  const float4 c0 = __ldg(pc), c1 = __ldg(pc + 1), c2 = __ldg(pc + 2);
+  g.Ax = a0.x; g.Ay = a0.y; g.Az = a0.z; g.ABx = a0.w; g.ABy = a1.x; g.ABz = a1.y;
+  g.a0 = __float_as_int(a1.z); g.b0 = __float_as_int(a1.w);
+  g.ab_off = __float_as_int(a2.x); g.ab_n = __float_as_int(a2.y);
+  g.a = __float_as_int(a2.z); g.b = __float_as_int(a2.w);
+  g.Cx = c0.x; g.Cy = c0.y; g.Cz = c0.z; g.CDx = c0.w; g.CDy = c1.x; g.CDz = c1.y;
+  g.c0 = __float_as_int(c1.z); g.d0 = __float_as_int(c1.w);
+  g.cd_off = __float_as_int(c2.x); g.cd_n = __float_as_int(c2.y);
+  g.c = __float_as_int(c2.z); g.d = __float_as_int(c2.w);
   return g;
 }
 
@@ -834,7 +856,7 @@ __device__ __forceinline__ void digest_t1(const KParams &kp, const QGeom<R> &g, 
                                           R scale, const R *__restrict__ D, double *Jh, double *Kh, int bra_key = -1) {
   using Q = QC<LA, LB, LC, LD>;
   const int n = kp.nao;
-  const int a0 = kp.sh.ao[g.a], b0 = kp.sh.ao[g.b], c0 = kp.sh.ao[g.c], d0 = kp.sh.ao[g.d];
+  const int a0 = g.a0, b0 = g.b0, c0 = g.c0, d0 = g.d0;
   R v[Q::NABCD];
 #pragma unroll
   for (int o = 0; o < Q::NABCD; ++o) v[o] = acc[o] * (R)Q::norm(o);
@@ -932,7 +954,7 @@ __device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
   using Q = QC<LA, LB, LC, LD>;
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
   const int n = kp.nao;
-  const int a0 = kp.sh.ao[g.a], b0 = kp.sh.ao[g.b], c0 = kp.sh.ao[g.c], d0 = kp.sh.ao[g.d];
+  const int a0 = g.a0, b0 = g.b0, c0 = g.c0, d0 = g.d0;
   __syncwarp(gmask);
 #pragma unroll
   for (int k = 0; k < Grp<LA, LB, LC, LD, R, T>::NPER; ++k) {
@@ -1021,7 +1043,7 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
       if (q >= w.n) return;
       const int sub = (int)(gid - q * W) * P + p;
       const int2 ij = __ldg(w.list + q);
-      const QGeom<R> g = make_geom<R>(kp, w.x0 + ij.x, w.y0 + ij.y, false, false);
+      const QGeom<R> g = make_geom32(kp, w.x0 + ij.x, w.y0 + ij.y);
       R scale = (R)1;
       if (g.a == g.b) scale *= (R)0.5;
       if (g.c == g.d) scale *= (R)0.5;
@@ -1041,7 +1063,9 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
   const int2 ij = __ldg(w.list + q);
   const int i = ij.x, j = ij.y;
   const int pab = w.x0 + i, pcd = w.y0 + j;
-  const QGeom<R> g = make_geom<R>(kp, pab, pcd, false, false);
+  QGeom<R> g;
+  if constexpr (std::is_same<R, float>::value) g = make_geom32(kp, pab, pcd);
+  else g = make_geom<R>(kp, pab, pcd, false, false);
   R scale = (R)1;
   if (g.a == g.b) scale *= (R)0.5;
   if (g.c == g.d) scale *= (R)0.5;
