@@ -165,9 +165,45 @@ __device__ __forceinline__ void rys_row_f32_s(const float *row, float s, float &
   }
 }
 
+// The one-point rule in closed form (classes with L <= 1): w = F0(x),
+// u = F1(x)/F0(x).  Below x = 1, F1 by its Taylor series
+// F1 = sum_k (-x)^k / (k! (2k+3)) (11 terms, truncation < 1e-8) and
+// F0 = 2x F1 + e^{-x} (the downward recursion); above, F0 = sqrt(pi/x)/2
+// erf(sqrt x) and F1 = (F0 - e^{-x}) / (2x).  No table rows are read.
+__device__ __forceinline__ void rys_n1_f32(float x, float &u, float &w) {
+  const float e = expf(-x);
+  float f0, f1;
+  if (x < 1.0f) {
+    f1 = 1.0f / 83462400.0f;
+    f1 = f1 * x - 1.0f / 7620480.0f;
+    f1 = f1 * x + 1.0f / 766080.0f;
+    f1 = f1 * x - 1.0f / 85680.0f;
+    f1 = f1 * x + 1.0f / 10800.0f;
+    f1 = f1 * x - 1.0f / 1560.0f;
+    f1 = f1 * x + 1.0f / 264.0f;
+    f1 = f1 * x - 1.0f / 54.0f;
+    f1 = f1 * x + 1.0f / 14.0f;
+    f1 = f1 * x - 1.0f / 5.0f;
+    f1 = f1 * x + 1.0f / 3.0f;
+    f0 = 2.0f * x * f1 + e;
+  } else {
+    const float sx = sqrtf(x);
+    f0 = 0.886226925452758f / sx * erff(sx);   // sqrt(pi) / 2
+    f1 = (f0 - e) / (2.0f * x);
+  }
+  w = f0;
+  u = f1 / f0;
+}
+
 template <int N>
 __device__ __forceinline__ void rys_roots_all_f32_s(const KParams &kp, const float *tab_s, float x, float (&u)[N],
                                                     float (&w)[N]) {
+  if constexpr (N == 1) {
+    if (x < (float)kTabXmax) {
+      rys_n1_f32(x, u[0], w[0]);
+      return;
+    }
+  }
   if (x >= (float)kTabXmax) {
     const float ix = 1.0f / x, isx = rsqrtf(x);
 #pragma unroll
@@ -186,6 +222,12 @@ __device__ __forceinline__ void rys_roots_all_f32_s(const KParams &kp, const flo
 
 template <int N>
 __device__ __forceinline__ void rys_roots_all_f32(const KParams &kp, float x, float (&u)[N], float (&w)[N]) {
+  if constexpr (N == 1) {
+    if (x < (float)kTabXmax) {
+      rys_n1_f32(x, u[0], w[0]);
+      return;
+    }
+  }
   if (x >= (float)kTabXmax) {
     const float ix = 1.0f / x, isx = rsqrtf(x);
 #pragma unroll
