@@ -42,6 +42,15 @@ __host__ __device__ constexpr int tgrad(int nabcd) {
   return nabcd <= 18 ? 1 : nabcd <= 27 ? 4 : nabcd <= 81 ? 8 : nabcd <= 216 ? 16 : 32;
 }
 
+// per arithmetic: FP32 values take half the registers, so the FP32 kernels
+// keep quartets of up to 27 outputs in one lane (measured: faster up to 27,
+// slower with fewer lanes beyond)
+template <typename R>
+__host__ __device__ constexpr int tgrad_r(int nabcd) {
+  if constexpr (sizeof(R) == sizeof(float)) return nabcd <= 27 ? 1 : tgrad(nabcd);
+  else return tgrad(nabcd);
+}
+
 template <int LA, int LB, int LC, int LD, typename R, int T>
 struct GGrp {
   using Q = QC<LA, LB, LC, LD>;
@@ -322,7 +331,7 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
 
 template <int LA, int LB, int LC, int LD, typename R>
 constexpr size_t grad_smem() {
-  constexpr int T = tgrad(QC<LA, LB, LC, LD>::NABCD);
+  constexpr int T = tgrad_r<R>(QC<LA, LB, LC, LD>::NABCD);
   return (T == 1 ? 0 : (size_t)(kBlock / T) * GGrp<LA, LB, LC, LD, R, T>::BUFN * sizeof(R)) +
          3 * kGradSmemAtoms * sizeof(double);
 }

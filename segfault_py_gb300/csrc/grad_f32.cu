@@ -9,7 +9,7 @@ namespace sf {
 
 template <int LA, int LB, int LC, int LD>
 static cudaError_t run_grad32(const KParams &kp, const ClassWork &w, const float *D, double *grad, cudaStream_t st) {
-  constexpr int T = tgrad(QC<LA, LB, LC, LD>::NABCD);
+  constexpr int T = tgrad_r<float>(QC<LA, LB, LC, LD>::NABCD);
   if (w.n <= 0) return cudaSuccess;
   // the split S = P*W chosen for the energy kernel's lanes, re-cut for this
   // kernel's T: as many sub-groups inside the T*P <= 32 lanes as fit, the rest
@@ -41,7 +41,7 @@ cudaError_t prepare_grad_f32() {
   cudaError_t e = cudaSuccess;
 #define SF_PREP(id, la, lb, lc, ld, t64, t32)                                                               \
   if (e == cudaSuccess)                                                                                     \
-    e = prep_smem(grad_kernel<la, lb, lc, ld, float, tgrad(QC<la, lb, lc, ld>::NABCD)>,                    \
+    e = prep_smem(grad_kernel<la, lb, lc, ld, float, tgrad_r<float>(QC<la, lb, lc, ld>::NABCD)>,                    \
                   grad_smem<la, lb, lc, ld, float>());
   SF_CLASS_LIST(SF_PREP)
 #undef SF_PREP
