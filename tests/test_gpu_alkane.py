@@ -20,11 +20,12 @@ def test_alkane_graph_mixed_vs_fp64(cuda):
     assert mol.nao == 510
     fb = FockBuilder(mol, device=cuda, cutoff=1e-12, fp32_cutoff=1e-2)
     ref = scf_diis(mol, tol=1e-9, dtol=1e-7, fb=fb, precision="fp64")
-    g = GraphSCF(mol, fb=fb, precision="mixed", fp32_cutoff=1e-2).capture()
-    r = g.run(tol=1e-9)
-    assert r.converged
-    assert abs(r.energy - ref.energy) < 1e-6
     g64 = rhf_gradient(mol, ref, fb, precision="fp64")
-    gmx = rhf_gradient(mol, ref, fb, precision="mixed")
-    assert float((gmx - g64).abs().max()) < 1e-6
+    for prec in ("mixed", "mixed_df"):
+        g = GraphSCF(mol, fb=fb, precision=prec, fp32_cutoff=1e-2).capture()
+        r = g.run(tol=1e-9)
+        assert r.converged
+        assert abs(r.energy - ref.energy) < 1e-6
+        gmx = rhf_gradient(mol, ref, fb, precision=prec)
+        assert float((gmx - g64).abs().max()) < 1e-6
     assert float(g64.sum(dim=0).abs().max()) < 1e-8

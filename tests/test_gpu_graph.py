@@ -17,7 +17,7 @@ def test_graph_scf_h2o_sto3g(cuda):
     assert abs(r.energy - (-74.96306315472287)) < 1e-9
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6), ("mixed_df", 1e-6)])
 def test_graph_scf_matches_eager(cuda, precision, tol):
     from segfault_py_gb300 import geometry as G
     from segfault_py_gb300.molecule import Molecule
