@@ -647,6 +647,16 @@ __device__ __forceinline__ double to_f64(float f) { return f2d_alu(f); }
 __device__ __forceinline__ double to_f64(double f) { return f; }
 __device__ __forceinline__ double to_f64(dd f) { return f2d_alu(f.hi) + f2d_alu(f.lo); }
 
+// advance the (ab, cd) primitive indices of a flattened index by step
+__device__ __forceinline__ void prim_advance(int &ip, int &iq, int step, int cd_n) {
+  iq += step;
+  if (iq >= cd_n) {
+    const int k = iq / cd_n;
+    ip += k;
+    iq -= k * cd_n;
+  }
+}
+
 // bra primitive-pair values cached across primitive quartets
 template <typename R>
 struct BraRec {
@@ -712,13 +722,16 @@ __device__ __forceinline__ void eval_t1_x2(const KParams &kp, const QGeom<R> &g,
   const int nprim = g.ab_n * g.cd_n;
   int cur = -1;
   BraRec<R> br;
+  // (ab, cd) primitive indices of idx advanced incrementally: a division
+  // only when the cd index wraps
+  int ip1 = p / g.cd_n, iq1 = p - ip1 * g.cd_n;
   for (int idx = p; idx < nprim; idx += 2 * P) {
     const bool two = idx + P < nprim;
-    const int j2 = two ? idx + P : idx;
-    const int ip1 = idx / g.cd_n, ip2 = j2 / g.cd_n;
+    int ip2 = ip1, iq2 = iq1;
+    if (two) prim_advance(ip2, iq2, P, g.cd_n);
     KetRec<R> k1, k2;
-    load_ket<R>(kp, g, idx - ip1 * g.cd_n, k1);
-    load_ket<R>(kp, g, j2 - ip2 * g.cd_n, k2);
+    load_ket<R>(kp, g, iq1, k1);
+    load_ket<R>(kp, g, iq2, k2);
     if (ip1 != cur) {
       load_bra<R>(kp, g, ip1, br);
       cur = ip1;
@@ -740,6 +753,7 @@ __device__ __forceinline__ void eval_t1_x2(const KParams &kp, const QGeom<R> &g,
     roots_t1<NR, R>(kp, tab_s, s2.x, u2, w2);
     assemble_pq<LA, LB, LC, LD, R>(g, s1, u1, w1, acc);
     assemble_pq<LA, LB, LC, LD, R>(g, s2, u2, w2, acc);
+    prim_advance(ip1, iq1, 2 * P, g.cd_n);
   }
 }
 
@@ -764,16 +778,20 @@ __device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R 
   // primitive quartets idx = p, p+P, ... of the ab-major flattened loop; the
   // ket record of the next one is loaded while this one is evaluated
   KetRec<R> kn;
-  if (p < nprim) load_ket<R>(kp, g, p % g.cd_n, kn);
+  int ip = p / g.cd_n, iq = p - ip * g.cd_n;   // (ab, cd) indices of idx
+  if (p < nprim) load_ket<R>(kp, g, iq, kn);
   for (int idx = p; idx < nprim; idx += P) {
-    const int ip = idx / g.cd_n;
     const KetRec<R> kc = kn;
-    if (idx + P < nprim) load_ket<R>(kp, g, (idx + P) % g.cd_n, kn);
+    int ipn = ip, iqn = iq;
+    prim_advance(ipn, iqn, P, g.cd_n);
+    if (idx + P < nprim) load_ket<R>(kp, g, iqn, kn);
     if (ip != cur) {
       load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
       cur = ip;
     }
     set_prim_cd<R>(g, kc, s, pp, px, py, pz, kab);
+    ip = ipn;
+    iq = iqn;
     R u[NR], w[NR];
     roots_t1<NR, R>(kp, tab_s, s.x, u, w);
 #pragma unroll
@@ -829,16 +847,20 @@ __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R
   PQ<R> s;
   R pp, px, py, pz, kab;
   KetRec<R> kn;
-  if (p < nprim) load_ket<R>(kp, g, p % g.cd_n, kn);
+  int ip = p / g.cd_n, iq = p - ip * g.cd_n;   // (ab, cd) indices of idx
+  if (p < nprim) load_ket<R>(kp, g, iq, kn);
   for (int idx = p; idx < nprim; idx += P) {
-    const int ip = idx / g.cd_n;
     const KetRec<R> kc = kn;
-    if (idx + P < nprim) load_ket<R>(kp, g, (idx + P) % g.cd_n, kn);
+    int ipn = ip, iqn = iq;
+    prim_advance(ipn, iqn, P, g.cd_n);
+    if (idx + P < nprim) load_ket<R>(kp, g, iqn, kn);
     if (ip != cur) {
       load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
       cur = ip;
     }
     set_prim_cd<R>(g, kc, s, pp, px, py, pz, kab);
+    ip = ipn;
+    iq = iqn;
     // each root once: lane t evaluates roots t, t+T, ... into the group buffer
     for (int r = t; r < NR; r += T) {
       R uu, ww;
