@@ -774,22 +774,31 @@ __device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R 
   const int nprim = g.ab_n * g.cd_n;
   int cur = -1;
   PQ<R> s;
-  R pp, px, py, pz, kab;
   // primitive quartets idx = p, p+P, ... of the ab-major flattened loop; the
-  // ket record of the next one is loaded while this one is evaluated
+  // ket record of the next one, and its bra record when the bra index
+  // changes, are loaded while this one is evaluated
   KetRec<R> kn;
+  BraRec<R> bn, b;
   int ip = p / g.cd_n, iq = p - ip * g.cd_n;   // (ab, cd) indices of idx
-  if (p < nprim) load_ket<R>(kp, g, iq, kn);
+  if (p < nprim) {
+    load_ket<R>(kp, g, iq, kn);
+    load_bra<R>(kp, g, ip, bn);
+  }
   for (int idx = p; idx < nprim; idx += P) {
     const KetRec<R> kc = kn;
+    if (ip != cur) {
+      b = bn;
+      cur = ip;
+      s.i2p = b.i2p;
+      s.pax = b.px - g.Ax; s.pay = b.py - g.Ay; s.paz = b.pz - g.Az;
+    }
     int ipn = ip, iqn = iq;
     prim_advance(ipn, iqn, P, g.cd_n);
-    if (idx + P < nprim) load_ket<R>(kp, g, iqn, kn);
-    if (ip != cur) {
-      load_prim_ab<R>(kp, g, ip, s, pp, px, py, pz, kab);
-      cur = ip;
+    if (idx + P < nprim) {
+      load_ket<R>(kp, g, iqn, kn);
+      if (ipn != ip) load_bra<R>(kp, g, ipn, bn);
     }
-    set_prim_cd<R>(g, kc, s, pp, px, py, pz, kab);
+    set_prim_cd<R>(g, kc, s, b.p, b.px, b.py, b.pz, b.kab);
     ip = ipn;
     iq = iqn;
     R u[NR], w[NR];
