@@ -233,8 +233,9 @@ int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *cha
  * run concurrently on streams forked from the caller's, so these times
  * overlap); on = 2: the launches are also serialised on the caller's stream,
  * so each time is that kernel alone; 0: off.  sf_slice_info
- * then reports, per launch ("slice" = one class in one precision), the work
- * and the device time of the last profiled build (waits for its events).
+ * then reports, per launch ("slice" = one class in one precision), the work,
+ * the device time of the last profiled build (waits for its events) and the
+ * launch's start after the build's start (a timeline of the concurrent build).
  * No counterpart in the reference (it only times whole SCF runs,
  * src/hf/utils.py:76-83). */
 typedef struct {
@@ -246,6 +247,8 @@ typedef struct {
     double flop_alg;
     float ms;                 /* device time of the last profiled launch      */
     int32_t threads_per_quartet;   /* lanes per quartet: Cartesian split T x primitive split (P lane groups x W groups) */
+    float start_ms;           /* start of the launch after the start of its build */
+    int32_t stream;           /* side stream of the launch (-1: serialised)     */
 } sf_slice_info;
 
 int sf_set_profiling(sf_handle *h, int32_t on);

@@ -54,7 +54,8 @@ class Stats(C.Structure):
 class SliceInfo(C.Structure):
     _fields_ = [("cls", C.c_int32), ("precision", C.c_int32), ("la", C.c_int32), ("lb", C.c_int32),
                 ("lc", C.c_int32), ("ld", C.c_int32), ("quartets", C.c_int64), ("prim_quartets", C.c_int64),
-                ("flop_alg", C.c_double), ("ms", C.c_float), ("threads_per_quartet", C.c_int32)]
+                ("flop_alg", C.c_double), ("ms", C.c_float), ("threads_per_quartet", C.c_int32),
+                ("start_ms", C.c_float), ("stream", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

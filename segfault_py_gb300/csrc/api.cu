@@ -207,9 +207,13 @@ struct sf_handle {
   std::vector<sf_tune_entry> tune;
   int profiling = 0;              // 1: per-slice events; 2: also serialise launches
   std::vector<cudaEvent_t> ev;   // 2 per slice while profiling
+  cudaEvent_t prof_t0 = nullptr;  // start of the last profiled build (launch start offsets)
   // side streams: the class launches of one build are independent (they only
   // add into Jh/Kh with atomics), so they are spread over kSideStreams
   // streams forked from and joined back into the caller's stream
+  // one hardware work queue per side stream needs CUDA_DEVICE_MAX_CONNECTIONS
+  // >= kSideStreams when the context is created (default 8: streams then
+  // share queues, and a launch waits behind another stream's launch)
   static constexpr int kSideStreams = 16;
   static constexpr int kHiStreams = 6;   // high-priority side streams (accurate tier of a mixed build)
   cudaStream_t side[kSideStreams] = {};
@@ -605,6 +609,19 @@ int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, d
   return SF_OK;
 }
 
+// events of the profiling modes: two per launch plus the build's start,
+// recorded on the caller's stream before the launches fork
+int profiling_events(sf_handle *h, cudaStream_t st) {
+  while (h->ev.size() < 2 * h->slices.size()) {
+    cudaEvent_t e;
+    SF_CK(cudaEventCreate(&e));
+    h->ev.push_back(e);
+  }
+  if (!h->prof_t0) SF_CK(cudaEventCreate(&h->prof_t0));
+  SF_CK(cudaEventRecord(h->prof_t0, st));
+  return SF_OK;
+}
+
 // FP32 / double-float copies of D needed by the current launch list
 int convert_density(sf_handle *h, const double *D, float *D32, cudaStream_t st, int *launches) {
   const size_t nn = (size_t)h->nao * h->nao;
@@ -960,6 +977,7 @@ void sf_destroy(sf_handle *h) {
   if (!h) return;
   DeviceGuard g(h->device);
   for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
+  if (h->prof_t0) cudaEventDestroy(h->prof_t0);
   for (int k = 0; k < sf_handle::kSideStreams; ++k) {
     if (h->side[k]) cudaStreamDestroy(h->side[k]);
     if (h->join_ev[k]) cudaEventDestroy(h->join_ev[k]);
@@ -989,10 +1007,14 @@ int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out) {
   out->flop_alg = s.flops;
   out->threads_per_quartet = (s.prec == 1 ? ci.t32 : ci.t64) * s.w.psplit * s.w.wsplit;
   out->ms = -1.0f;
+  out->start_ms = -1.0f;
+  out->stream = (h->profiling == 2 || (size_t)idx >= h->slice_stream.size()) ? -1 : h->slice_stream[idx];
   if (h->profiling && h->ev.size() >= 2 * h->slices.size()) {
     SF_CK(cudaEventSynchronize(h->ev[2 * idx + 1]));
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, h->ev[2 * idx], h->ev[2 * idx + 1]) == cudaSuccess) out->ms = ms;
+    else cudaGetLastError();
+    if (h->prof_t0 && cudaEventElapsedTime(&ms, h->prof_t0, h->ev[2 * idx]) == cudaSuccess) out->start_ms = ms;
     else cudaGetLastError();
   }
   return SF_OK;
@@ -1073,12 +1095,9 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
   int launches = 0;
   rc = convert_density(h, D, h->d_D32.p, st, &launches);
   if (rc) return rc;
-  if (h->profiling && h->ev.size() < 2 * h->slices.size()) {
-    while (h->ev.size() < 2 * h->slices.size()) {
-      cudaEvent_t e;
-      SF_CK(cudaEventCreate(&e));
-      h->ev.push_back(e);
-    }
+  if (h->profiling) {
+    rc = profiling_events(h, st);
+    if (rc) return rc;
   }
   rc = launch_slices(h, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st, h->profiling, &launches);
   if (rc) return rc;
@@ -1352,11 +1371,8 @@ int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, d
     return launch_grad_dd(s.cls, h->kp, s.w, reinterpret_cast<const dd *>(h->d_Ddd.p), grad, ss);
   };
   if (h->profiling) {   // per-launch events (serialised in mode 2), read by sf_get_slice_info
-    while (h->ev.size() < 2 * h->slices.size()) {
-      cudaEvent_t e;
-      SF_CK(cudaEventCreate(&e));
-      h->ev.push_back(e);
-    }
+    const int rc = profiling_events(h, st);
+    if (rc) return rc;
     if (h->profiling == 2) {
       for (size_t k = 0; k < h->slices.size(); ++k) {
         SF_CK(cudaEventRecord(h->ev[2 * k], st));

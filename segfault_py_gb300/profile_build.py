@@ -8,8 +8,10 @@ on the Schwarz bounds) and runs `--builds` Fock builds.  With `--slices` the
 library serialises its launches on one stream and times each with CUDA events;
 the table lists, per launch (one class, precision and lanes-per-quartet
 segment), the quartets, primitive quartets, device time, share of the build
-and algorithmic GFLOP/s.  Without `--slices` it only runs the builds (the
-command to put under a profiler).
+and algorithmic GFLOP/s.  With `--timeline` the launches stay concurrent and
+each one's start and end after the start of the build are listed, with the
+number of launches in flight over time.  Without either it only runs the
+builds (the command to put under a profiler).
 """
 from __future__ import annotations
 
@@ -45,6 +47,30 @@ def slice_table(fb: FockBuilder):
     return tot, rows
 
 
+def timeline_table(fb: FockBuilder, bin_ms: float = 0.05):
+    sl = sorted(fb.slice_info(), key=lambda q: q["start_ms"])
+    span = max(q["start_ms"] + q["ms"] for q in sl)
+    busy = sum(q["ms"] for q in sl)
+    rows = ["build span %.4f ms, launch time summed %.4f ms (mean launches in flight %.2f)" % (span, busy, busy / span)]
+    for kind, name in ((0, "f64"), (1, "f32"), (2, "dd")):
+        k = [q for q in sl if q["precision"] == kind]
+        if k:
+            rows.append("  %s: %d launches, first start %.4f ms, last end %.4f ms, summed %.4f ms" % (
+                name, len(k), min(q["start_ms"] for q in k), max(q["start_ms"] + q["ms"] for q in k),
+                sum(q["ms"] for q in k)))
+    nb = int(span / bin_ms) + 1
+    occ = []
+    for b in range(nb):
+        t0, t1 = b * bin_ms, (b + 1) * bin_ms
+        occ.append(sum(max(0.0, min(t1, q["start_ms"] + q["ms"]) - max(t0, q["start_ms"])) for q in sl) / bin_ms)
+    rows.append("launches in flight per %.3f ms bin: %s" % (bin_ms, " ".join("%.1f" % o for o in occ)))
+    for q in sl:
+        rows.append("start=%8.4f end=%8.4f stream=%2d (%d%d|%d%d) %s T=%2d q=%9d ms=%8.4f" % (
+            q["start_ms"], q["start_ms"] + q["ms"], q["stream"], q["la"], q["lb"], q["lc"], q["ld"],
+            ("f64", "f32", "dd")[q["precision"]], q["threads_per_quartet"], q["quartets"], q["ms"]))
+    return rows
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--nwater", type=int, default=8)
@@ -54,6 +80,8 @@ def main(argv=None):
     ap.add_argument("--fp32-cutoff", type=float, default=1e-2)
     ap.add_argument("--builds", type=int, default=3)
     ap.add_argument("--slices", action="store_true")
+    ap.add_argument("--timeline", action="store_true",
+                    help="concurrent launches with start/end times (last build)")
     ap.add_argument("--time", action="store_true", help="also time --builds normal (concurrent) builds with events")
     ap.add_argument("--autotune", action="store_true", help="autotune the launch shapes first")
     ap.add_argument("--grad", action="store_true",
@@ -70,6 +98,8 @@ def main(argv=None):
         print("autotuned %d launches, serialised time saved %.4f ms" % (len(tab), gain))
     if a.slices:
         fb.set_profiling(2)
+    elif a.timeline:
+        fb.set_profiling(1)
     if a.grad:
         from . import _lib
         from .fock import _ptr, _stream_ptr
@@ -87,6 +117,8 @@ def main(argv=None):
         tot, rows = slice_table(fb)
         print("serialised kernel time of one build: %.4f ms" % tot)
         print("\n".join(rows))
+    if a.timeline and not a.slices:
+        print("\n".join(timeline_table(fb)))
     if a.time and not a.grad:
         fb.set_profiling(0)
         J = torch.empty_like(D)
