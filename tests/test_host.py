@@ -136,3 +136,52 @@ def test_nuclear_repulsion_gradient_fd():
             xm[a, d] -= h * BOHR
             fd = (Molecule.from_geometry(s, xp, "sto-3g").e_nuc - Molecule.from_geometry(s, xm, "sto-3g").e_nuc) / (2 * h)
             assert abs(fd - g[a, d]) < 1e-7
+
+
+def test_ctypes_structs_match_header_layout(tmp_path):
+    """Every struct of include/segfock.h that the binding mirrors has the
+    same size and field offsets in C (gcc on the header) and in ctypes."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from segfault_py_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"sf_shell_desc": _lib.ShellDesc, "sf_stats": _lib.Stats, "sf_slice_info": _lib.SliceInfo,
+               "sf_tune_entry": _lib.TuneEntry}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "segfock.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", f"{REPO}/include", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_timeline_table_bins_and_tiers():
+    from segfault_py_gb300.profile_build import timeline_table
+
+    class FakeBuilder:
+        def slice_info(self):
+            base = {"la": 0, "lb": 0, "lc": 0, "ld": 0, "threads_per_quartet": 1, "quartets": 10}
+            return [dict(base, start_ms=0.0, ms=0.1, precision=1, stream=0),
+                    dict(base, start_ms=0.05, ms=0.1, precision=2, stream=1),
+                    dict(base, start_ms=0.15, ms=0.05, precision=1, stream=0)]
+
+    rows = timeline_table(FakeBuilder(), bin_ms=0.05)
+    assert rows[0].startswith("build span 0.2000 ms, launch time summed 0.2500 ms")
+    assert "f32: 2 launches, first start 0.0000 ms, last end 0.2000 ms, summed 0.1500 ms" in rows[1]
+    assert "dd: 1 launches, first start 0.0500 ms, last end 0.1500 ms, summed 0.1000 ms" in rows[2]
+    # bins [0,.05) [.05,.1) [.1,.15) [.15,.2) [.2,.25): 1, 2, 1, 1, 0 launches in flight
+    assert rows[3].endswith("1.0 2.0 1.0 1.0 0.0")
+    assert [r.split()[0] for r in rows[4:]] == ["start=", "start=", "start="]
