@@ -205,8 +205,12 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    clk_path = os.path.join(REPO, "gpurun_out", "bench_clocks_rank%d.csv" % rank)
-    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    if args.clocks_log:
+        clk_path = args.clocks_log
+    else:
+        import tempfile
+        clk_path = os.path.join(tempfile.gettempdir(), "segfock_bench_clocks_rank%d.csv" % rank)
+    os.makedirs(os.path.dirname(os.path.abspath(clk_path)), exist_ok=True)
     proc, fh = clock_sampler_start(clk_path) if rank == 0 else (None, None)
     t_hl = time_steps(lambda: fb.jk(D, precision=HEADLINE, out=(J, K)), args.steps, args.warmup, flush, stream)
     t_mx = time_steps(lambda: fb.jk(D, precision="mixed", out=(J, K)), args.steps, args.warmup, flush, stream)
@@ -525,6 +529,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--eri-quartets", type=int, default=1_000_000, help="raw-ERI stress batch size (0: off)")
     ap.add_argument("--no-alkane", dest="alkane", action="store_false", help="skip the C20H42 6-31G** block")
+    ap.add_argument("--clocks-log", default=None,
+                    help="CSV of the nvidia-smi clock samples taken during the timed region (default: a temporary file)")
     ap.add_argument("--tuning", default=None,
                     help="launch-shape table of the headline cluster: loaded when the file exists (no autotuning), "
                          "else written after autotuning")
