@@ -169,7 +169,9 @@ __device__ __forceinline__ void rys_row_f32_s(const float *row, float s, float &
 // u = F1(x)/F0(x).  Below x = 1, F1 by its Taylor series
 // F1 = sum_k (-x)^k / (k! (2k+3)) (11 terms, truncation < 1e-8) and
 // F0 = 2x F1 + e^{-x} (the downward recursion); above, F0 = sqrt(pi/x)/2
-// erf(sqrt x) and F1 = (F0 - e^{-x}) / (2x).  No table rows are read.
+// erf(sqrt x) and F1 = (F0 - e^{-x}) / (2x).  No table rows are read.  The
+// square root and the quotients use the approximate reciprocal forms
+// (rsqrtf, __fdividef: within 2 ulp), far inside the FP32 tier's error.
 __device__ __forceinline__ void rys_n1_f32(float x, float &u, float &w) {
   const float e = expf(-x);
   float f0, f1;
@@ -187,12 +189,12 @@ __device__ __forceinline__ void rys_n1_f32(float x, float &u, float &w) {
     f1 = f1 * x + 1.0f / 3.0f;
     f0 = 2.0f * x * f1 + e;
   } else {
-    const float sx = sqrtf(x);
-    f0 = 0.886226925452758f / sx * erff(sx);   // sqrt(pi) / 2
-    f1 = (f0 - e) / (2.0f * x);
+    const float isx = rsqrtf(x), sx = x * isx;
+    f0 = 0.886226925452758f * isx * erff(sx);   // sqrt(pi) / 2
+    f1 = __fdividef(f0 - e, 2.0f * x);
   }
   w = f0;
-  u = f1 / f0;
+  u = __fdividef(f1, f0);
 }
 
 template <int N>
@@ -205,7 +207,7 @@ __device__ __forceinline__ void rys_roots_all_f32_s(const KParams &kp, const flo
     }
   }
   if (x >= (float)kTabXmax) {
-    const float ix = 1.0f / x, isx = rsqrtf(x);
+    const float ix = __fdividef(1.0f, x), isx = rsqrtf(x);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       u[i] = kp.asym32.r[N][i] * ix;
@@ -229,7 +231,7 @@ __device__ __forceinline__ void rys_roots_all_f32(const KParams &kp, float x, fl
     }
   }
   if (x >= (float)kTabXmax) {
-    const float ix = 1.0f / x, isx = rsqrtf(x);
+    const float ix = __fdividef(1.0f, x), isx = rsqrtf(x);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       u[i] = kp.asym32.r[N][i] * ix;
@@ -362,7 +364,7 @@ template <int N, typename R>
 __device__ __forceinline__ void rys_root_one(const KParams &kp, R x, int r, R &u, R &w) {
   if constexpr (std::is_same<R, float>::value) {
     if (x >= (float)kTabXmax) {
-      u = kp.asym32.r[N][r] / x;
+      u = __fdividef(kp.asym32.r[N][r], x);
       w = kp.asym32.w[N][r] * rsqrtf(x);
       return;
     }
