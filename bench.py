@@ -152,6 +152,20 @@ def time_steps(fn, steps, warmup, flush, stream):
     return [a.elapsed_time(b) for a, b in ev]
 
 
+def dominant_kernel(slices):
+    """The J/K class kernel with the most device time over its launches of one
+    build (launches of one class and precision run the same kernel), its
+    largest launch and its name: (largest launch, all its launches, name)."""
+    groups = {}
+    for sl in slices:
+        groups.setdefault((sl["la"], sl["lb"], sl["lc"], sl["ld"], sl["precision"]), []).append(sl)
+    group = max(groups.values(), key=lambda g: sum(sl["ms"] for sl in g))
+    top = max(group, key=lambda sl: sl["ms"])
+    name = "jk_kernel<%d,%d,%d,%d,%s>" % (top["la"], top["lb"], top["lc"], top["ld"],
+                                          ("fp64", "fp32", "dd")[top["precision"]])
+    return top, group, name
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -260,13 +274,7 @@ def run_ours(args):
     # roofline of the dominant class kernel of the headline build (double-float
     # kernels run on the FP32 pipe: their FP64-equivalent algorithmic FLOPs are
     # set against the FP32 FMA peak)
-    # launches of one (class, precision) run the same kernel; the kernel with
-    # the most device time is the dominant one, its largest launch is timed
-    groups = {}
-    for sl in slices_hl:
-        groups.setdefault((sl["la"], sl["lb"], sl["lc"], sl["ld"], sl["precision"]), []).append(sl)
-    dom_group = max(groups.values(), key=lambda g: sum(sl["ms"] for sl in g))
-    dom = max(dom_group, key=lambda sl: sl["ms"])
+    dom, dom_group, dom_name = dominant_kernel(slices_hl)
     dom_ms = sum(sl["ms"] for sl in dom_group)
     kind = ("fp64", "fp32", "dd")[dom["precision"]]
     pipe = "fp64" if kind == "fp64" else "fp32"
@@ -285,7 +293,6 @@ def run_ours(args):
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(mol, args.cpu_seconds)
-    dom_name = "jk_kernel<%d,%d,%d,%d,%s>" % (dom["la"], dom["lb"], dom["lc"], dom["ld"], kind)
     rec = {
         "metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": ms_hl / steps, "higher_is_better": True, "scaling": "weak",

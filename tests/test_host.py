@@ -185,3 +185,20 @@ def test_timeline_table_bins_and_tiers():
     # bins [0,.05) [.05,.1) [.1,.15) [.15,.2) [.2,.25): 1, 2, 1, 1, 0 launches in flight
     assert rows[3].endswith("1.0 2.0 1.0 1.0 0.0")
     assert [r.split()[0] for r in rows[4:]] == ["start=", "start=", "start="]
+
+
+def test_bench_dominant_kernel_sums_launches_of_one_kernel():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", f"{REPO}/bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    def sl(cls, prec, ms, flop=1.0):
+        return {"la": cls[0], "lb": cls[1], "lc": cls[2], "ld": cls[3], "precision": prec, "ms": ms,
+                "flop_alg": flop, "threads_per_quartet": 1}
+
+    slices = [sl((2, 0, 1, 1), 2, 0.05), sl((1, 0, 0, 0), 1, 0.03), sl((1, 0, 0, 0), 1, 0.04),
+              sl((1, 0, 0, 0), 2, 0.02)]
+    top, group, name = bench.dominant_kernel(slices)
+    assert name == "jk_kernel<1,0,0,0,fp32>" and name in bench.NCU_TRAFFIC
+    assert len(group) == 2 and top["ms"] == 0.04
