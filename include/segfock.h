@@ -139,7 +139,9 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
  * for the given precision mode and cutoffs, on `stream` (adding into the
  * handle's scratch only; the caller's matrices are not touched):
  *   1. times whole builds (launches concurrent) with fill targets 0, 1/4, 1
- *      and 4 times 8 warps per SM sub-partition and keeps the fastest;
+ *      and 4 times 8 warps per SM sub-partition and keeps the fastest; in
+ *      the mixed modes it then times the accurate tier (few, long quartets)
+ *      at its own targets 0 .. 16 times, keeping one only if faster;
  *   2. times every launch alone (reps times) with S/4, S/2, S, 2S, 4S and
  *      records the fastest; streams are then assigned by measured times;
  *   3. keeps the step-2 splits only if the whole build got faster.
@@ -147,10 +149,11 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
  * number of launches tuned (>= 0) or an error code.  The table can be read
  * out and loaded again (e.g. from a file): sf_set_tuning replaces it (n = 0
  * clears it).  Entries with cls = -1 hold the fill target of precision mode
- * `precision` in `split` (quarters; 0 = no extra split). */
+ * `precision` in `split` (quarters; 0 = no extra split), entries with
+ * cls = -2 that of the accurate tier of a mixed mode when it differs. */
 typedef struct {
-    int32_t cls;           /* canonical class 0..20 (ss|ss .. dd|dd); -1: fill target */
-    int32_t precision;     /* launch kind: 0 FP64, 1 FP32, 2 double-float     */
+    int32_t cls;           /* canonical class 0..20 (ss|ss .. dd|dd); -1 / -2: fill target */
+    int32_t precision;     /* launch kind: 0 FP64, 1 FP32, 2 double-float; precision mode for cls < 0 */
     int64_t cost;          /* K_ab*K_cd of the launch's first (costliest) quartet */
     int32_t split;         /* chosen S = P*W (power of two)                   */
     float ms_default;      /* measured time with the rule's S                 */

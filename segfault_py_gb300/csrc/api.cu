@@ -229,6 +229,8 @@ struct sf_handle {
   // launch-fill target per precision mode, in quarters of "8 resident warps
   // per SM sub-partition" (0: no extra primitive split); set by sf_autotune
   int fill_x4[5] = {4, 4, 4, 4, 4};
+  // fill target of the accurate tier of a mixed mode (-1: fill_x4 of the mode)
+  int fill_acc_x4[5] = {-1, -1, -1, -1, -1};
   KParams kp;
 };
 
@@ -435,7 +437,8 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       // sub-partition's FP64 unit for 64 cycles): its quartets' primitive
       // loops are split further, up to S_fill = P*W sub-groups per quartet,
       // each sub-group keeping at least one primitive quartet
-      const int64_t fill = (int64_t)std::max(h->nsm, 1) * 4 * 8 * 32 * h->fill_x4[prec] / 4;
+      const int fx4 = (pr == 0 && h->fill_acc_x4[prec] >= 0) ? h->fill_acc_x4[prec] : h->fill_x4[prec];
+      const int64_t fill = (int64_t)std::max(h->nsm, 1) * 4 * 8 * 32 * fx4 / 4;
       int sfill = 1;
       while (p.n * T * sfill < fill && sfill < pmax * kMaxWsplit) sfill *= 2;
       auto split_of = [&](int64_t cost) {
@@ -1175,7 +1178,7 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
     std::vector<sf_tune_entry> keep;
     const int kinds[2] = {(precision == SF_PREC_MIXED_DF || precision == SF_PREC_DF) ? 2 : 0, 1};
     for (const auto &x : h->tune) {
-      bool mine = x.cls == -1 ? x.precision == precision : false;
+      bool mine = x.cls < 0 ? x.precision == precision : false;
       if (x.cls >= 0)
         for (int k : kinds)
           if (x.precision == k &&
@@ -1189,6 +1192,7 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
   // 1. the launch-fill target of this mode, by whole-build time (per-launch
   // splits of this mode cleared first)
   drop_entries();
+  h->fill_acc_x4[precision] = -1;
   int best_fill = h->fill_x4[precision];
   float best_ms = 1e30f;
   for (int f : {0, 1, 4, 16}) {
@@ -1207,6 +1211,28 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
     }
   }
   h->fill_x4[precision] = best_fill;
+  // mixed modes: the accurate tier's few quartets fill the GPU at another
+  // target than the FP32 tier's many; searched with the FP32 tier's fixed
+  int best_acc = -1;
+  if (precision == SF_PREC_MIXED || precision == SF_PREC_MIXED_DF) {
+    for (int f : {0, 1, 4, 16, 64}) {
+      if (f == best_fill) continue;   // already timed: the mode's target for both tiers
+      h->fill_acc_x4[precision] = f;
+      h->c_prec = -1;
+      float ms = 0.f;
+      rc = time_build(&ms);
+      if (rc) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_acc = f;
+      }
+    }
+    h->fill_acc_x4[precision] = best_acc;
+  }
   h->c_prec = -1;
   rc = build_work(h, precision, cutoff, fp32_cutoff);
   if (rc) {
@@ -1270,6 +1296,8 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
     tuned = 0;
   }
   h->tune.push_back(sf_tune_entry{-1, precision, 0, best_fill, best_ms, std::min(best_ms, tuned_ms)});
+  if (best_acc >= 0)
+    h->tune.push_back(sf_tune_entry{-2, precision, 0, best_acc, best_ms, std::min(best_ms, tuned_ms)});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   h->c_prec = -1;   // the next build re-cuts the lists and assigns streams by the measured times
@@ -1288,17 +1316,22 @@ int sf_set_tuning(sf_handle *h, const sf_tune_entry *entries, int32_t n) {
   if (!h || n < 0 || (n > 0 && !entries)) return fail(SF_EINVAL, "sf_set_tuning: bad arguments");
   for (int32_t i = 0; i < n; ++i) {
     const sf_tune_entry &e = entries[i];
-    const bool fill_entry = e.cls == -1 && e.precision >= 0 && e.precision <= SF_PREC_DF && e.split >= 0 &&
-                            e.split <= 64;
+    const bool fill_entry = (e.cls == -1 || e.cls == -2) && e.precision >= 0 && e.precision <= SF_PREC_DF &&
+                            e.split >= 0 && e.split <= 64;
     if (fill_entry) continue;
     if (e.cls < 0 || e.cls >= kNumClass || e.precision < 0 || e.precision > 2 || e.split < 1 ||
         e.split > 32 * kMaxWsplit || (e.split & (e.split - 1)))
       return fail(SF_EINVAL, "sf_set_tuning: bad entry " + std::to_string(i));
   }
   h->tune.assign(entries, entries + n);
-  for (int m = 0; m <= SF_PREC_DF; ++m) h->fill_x4[m] = 4;
-  for (const auto &e : h->tune)
+  for (int m = 0; m <= SF_PREC_DF; ++m) {
+    h->fill_x4[m] = 4;
+    h->fill_acc_x4[m] = -1;
+  }
+  for (const auto &e : h->tune) {
     if (e.cls == -1) h->fill_x4[e.precision] = e.split;
+    if (e.cls == -2) h->fill_acc_x4[e.precision] = e.split;
+  }
   h->c_prec = -1;   // rebuild the launch list with the new splits
   return SF_OK;
 }

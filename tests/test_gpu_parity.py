@@ -269,6 +269,8 @@ def test_autotune_keeps_results(cuda, tmp_path):
         J0, K0 = fb.jk(D, precision=prec)
         table = fb.autotune(D, precision=prec, reps=2)
         assert any(e["cls"] == -1 for e in table)
+        # an accurate-tier fill target only for the mixed modes (2, 3)
+        assert all(e["precision"] in (2, 3) and 0 <= e["split"] <= 64 for e in table if e["cls"] == -2)
         assert all(e["split"] >= 1 and (e["split"] & (e["split"] - 1)) == 0 for e in table if e["cls"] >= 0)
         J1, K1 = fb.jk(D, precision=prec)
         tol = 1e-12 if prec == "fp64" else 1e-6
