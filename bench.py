@@ -62,7 +62,9 @@ L2_FLUSH_BYTES = 256 << 20
 # workload, from one ncu capture each (profiles/ncu_jk_kernels_water8_631gs.md);
 # the roofline's "traffic" when the dominant kernel is one of them
 NCU_TRAFFIC = {"jk_kernel<2,0,1,0,fp32>": 2321664, "jk_kernel<2,0,0,0,dd>": 585984,
-               "jk_kernel<1,0,0,0,fp32>": 6875904, "jk_kernel<0,0,0,0,fp32>": 5513728}
+               "jk_kernel<1,0,0,0,fp32>": 6871296, "jk_kernel<0,0,0,0,fp32>": 5513728,
+               "jk_kernel<1,1,1,0,dd>": 336380, "jk_kernel<2,0,1,1,dd>": 374780,
+               "jk_kernel<2,1,1,0,dd>": 454660}
 
 
 def workload(nwater=8, basis="6-31g*", seed=0):
