@@ -34,7 +34,8 @@ Reported:
                and errors against FP64, Fock builds/s and forces/s
 
 ``--impl reference`` times the reference's CPU algorithm (oracle port, all host
-cores) on the same workload and prints the same metric.
+cores, the reference's root5 fits where transcribed) on the same workload and
+prints the same metric; every timed step there is one whole Fock build.
 Multi-GPU (torchrun, N ranks): replicas -- every rank builds the same Fock
 matrix; value = sum over ranks of builds / max-over-ranks time (weak scaling).
 """
@@ -58,13 +59,44 @@ HEADLINE = "mixed_df"
 CUTOFF = 1e-12
 FP32_CUTOFF = 1e-2
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of the largest launch of J/K class kernels of this
-# workload, from one ncu capture each (profiles/ncu_jk_kernels_water8_631gs.md);
-# the roofline's "traffic" when the dominant kernel is one of them
-NCU_TRAFFIC = {"jk_kernel<2,0,1,0,fp32>": 2321664, "jk_kernel<2,0,0,0,dd>": 585984,
-               "jk_kernel<1,0,0,0,fp32>": 6871296, "jk_kernel<0,0,0,0,fp32>": 5513728,
-               "jk_kernel<1,1,1,0,dd>": 336380, "jk_kernel<2,0,1,1,dd>": 374780,
-               "jk_kernel<2,1,1,0,dd>": 454660}
+# DRAM bytes (read + write) per launch of J/K class kernels of this workload,
+# from ncu captures committed as a text table under profiles/ together with a
+# hash of the kernel sources they were measured on; a table whose hash does
+# not match the sources being run gives traffic = null (stale)
+TRAFFIC_TABLE = os.path.join(REPO, "profiles", "ncu_dram_bytes_water8_631gs.txt")
+
+
+def csrc_hash():
+    """sha256 (first 16 hex digits) over the library's CUDA/C++ sources."""
+    import hashlib
+    d = os.path.join(REPO, "segfault_py_gb300", "csrc")
+    h = hashlib.sha256()
+    for f in sorted(os.listdir(d)):
+        if f.endswith((".cu", ".cuh", ".h", ".cpp")):
+            h.update(f.encode())
+            with open(os.path.join(d, f), "rb") as fh:
+                h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def ncu_traffic(kernel):
+    """(bytes per launch, source note) of a kernel from the committed table."""
+    if not os.path.exists(TRAFFIC_TABLE):
+        return None, "no ncu table"
+    table, src_hash = {}, None
+    for line in open(TRAFFIC_TABLE):
+        t = line.split()
+        if not t:
+            continue
+        if t[0] == "#" and len(t) >= 3 and t[1] == "csrc_sha16":
+            src_hash = t[2]
+        elif t[0] != "#" and len(t) >= 2:
+            table[t[0]] = float(t[1])
+    if src_hash != csrc_hash():
+        return None, "ncu table measured on other kernel sources (stale)"
+    if kernel not in table:
+        return None, "kernel not in the ncu table"
+    return table[kernel], "ncu capture, " + os.path.relpath(TRAFFIC_TABLE, REPO)
 
 
 def workload(nwater=8, basis="6-31g*", seed=0):
@@ -284,6 +316,8 @@ def run_ours(args):
     total_ms = sum(s["ms"] for s in slices_hl)
     comb = st_hl["flop_alg_fp32"] / (peaks["fp32"] * 1e12) + st_hl["flop_alg_fp64"] / (peaks["fp32"] * 1e12)
     build_frac = comb / (float(np.mean(t_hl)) * 1e-3)
+    traffic, traffic_src = ncu_traffic(dom_name)
+    setup = setup_costs(mol, dev, D, J, K)
     nn = mol.nao * mol.nao * 8
     secondary = None
     if args.nwater2 > 0:
@@ -321,10 +355,11 @@ def run_ours(args):
                    "max_grad_error_mixed_vs_fp64": grad_err, "unit_error": "Eh/bohr",
                    "note": "derivative integrals: FP32 below the cutoff, double-float above"},
         "autotune_s": tune_s,
+        "setup": setup,
         "gpu_launches": (int(st_hl["launches"]) * 3 + int(st_64["launches"])) * steps,
         "roofline": {"bound": pipe, "achieved": achieved, "peak": peaks[pipe], "unit": "TFLOP/s",
                      "frac": achieved / peaks[pipe] if peaks[pipe] else None,
-                     "traffic": NCU_TRAFFIC.get(dom_name), "traffic_unit": "bytes per launch (ncu)",
+                     "traffic": traffic, "traffic_unit": "bytes per launch (ncu)", "traffic_source": traffic_src,
                      "kernel": dom_name, "kernel_launches": len(dom_group),
                      "lanes_per_quartet": dom["threads_per_quartet"],
                      "kernel_share": dom_ms / total_ms if total_ms else None,
@@ -342,6 +377,38 @@ def run_ours(args):
 
 
 # ----------------------------------------------------------------------------
+def setup_costs(mol, dev, D, J, K, reps=3):
+    """Per-geometry cost, paid once per geometry (each step of an optimisation
+    or MD loop), outside the Fock-build timing: a new handle (shell and pair
+    tables, device upload), the Schwarz bounds (GPU kernels, then the pair
+    sort on the host) and the quartet lists the first build cuts on the host."""
+    import torch
+    from segfault_py_gb300.fock import FockBuilder
+    out = {"handle_and_schwarz_ms": [], "first_build_ms": [], "steady_build_ms": []}
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fb = FockBuilder(mol, device=dev, cutoff=CUTOFF, fp32_cutoff=FP32_CUTOFF, precision=HEADLINE)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        fb.jk(D, out=(J, K))
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        fb.jk(D, out=(J, K))
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        fb.close()
+        out["handle_and_schwarz_ms"].append((t1 - t0) * 1e3)
+        out["first_build_ms"].append((t2 - t1) * 1e3)
+        out["steady_build_ms"].append((t3 - t2) * 1e3)
+    m = {k: float(np.median(v)) for k, v in out.items()}
+    return {"handle_and_schwarz_ms": m["handle_and_schwarz_ms"],
+            "quartet_lists_ms": m["first_build_ms"] - m["steady_build_ms"],
+            "note": "per geometry, host wall clock (median of %d): sf_create + sf_schwarz, then the quartet lists "
+                    "cut by the first sf_fock_jk (first build minus a steady build, %s mode, untuned)"
+                    % (reps, HEADLINE)}
+
+
 def secondary_config(nwater, basis, steps, warmup, flush, dev):
     """Mixed (FP32 + double-float, and FP32 + FP64) vs FP64 Fock builds and
     forces on a second cluster size, launch shapes autotuned first."""
@@ -495,7 +562,12 @@ def cpu_baseline(mol, seconds=15.0):
 
 
 def run_reference(args):
-    """The reference's CPU algorithm (oracle port) on the host cores."""
+    """The reference's CPU algorithm (oracle port of core.f90 rys.eri_rys per
+    unique AO quartet, hf.py:33-61, with the reference's own root5 fits where
+    they were transcribed) on all host cores.  Every timed step is one whole
+    Fock build: all N(N+1)/2 x (N(N+1)/2 + 1)/2 unique AO quartets digested
+    into J and K.  The untimed warm-up steps run a 1/40 row sample each (they
+    only bring the code and tables into the caches)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -508,18 +580,13 @@ def run_reference(args):
     tot = npair * (npair + 1) // 2
     threads = os.cpu_count() or 1
     use_ref = O.use_reference_root5(True)
-    stride = 40 if n > 100 else 1
-    rows = np.arange(0, npair, stride)
+    for i in range(args.warmup):
+        O.jk_direct(cg, D, nthreads=threads, stride=40, phase=i % 40)
     times = []
-    for i in range(args.warmup + args.steps):
-        phase = i % stride
-        rows = np.arange(phase, npair, stride)
-        cov = int(np.sum(rows + 1))
+    for _ in range(args.steps):
         t = time.time()
-        O.jk_direct(cg, D, nthreads=threads, stride=stride, phase=phase)
-        dt = time.time() - t
-        if i >= args.warmup:
-            times.append(dt * tot / cov)
+        O.jk_direct(cg, D, nthreads=threads)
+        times.append(time.time() - t)
     full = float(np.mean(times))
     value = 1.0 / full
     rec = {"metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
@@ -527,8 +594,9 @@ def run_reference(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "impl": "reference",
            "config": cfg_dict(mol, args.nwater, args.basis),
            "cpu_baseline": {"value": value, "unit": "Fock builds/s", "cores": threads, "kind": "port",
-                            "sample": "each step: 1/%d of the packed pair rows (unique AO quartets), extrapolated"
-                                      % stride,
+                            "sample": "each timed step: one whole Fock build, all %d unique AO quartets "
+                                      "(warm-up steps: 1/40 of the pair rows)" % tot,
+                            "step_s": [round(v, 3) for v in times],
                             "roots": "reference root5 (transcribed)" if use_ref else "oracle root table"},
            "e2e": {"value": value, "unit": "Fock builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(rec))

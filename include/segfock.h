@@ -279,10 +279,16 @@ int sf_fma_peak(int32_t precision, double *flops, float *ms, void *stream);
  * The call allocates nothing: no cudaMalloc, cudaFree or allocating library
  * routine.  Set-up that does allocate must happen before it: sf_create,
  * sf_schwarz, and one sf_fock_jk call with the same precision and cutoffs,
- * which builds the quartet lists of the handle (otherwise SF_ESTATE).  The
+ * which builds the quartet lists of the handle (otherwise SF_ESTATE).
+ * sf_schwarz, sf_autotune, sf_set_tuning and sf_set_partition discard those
+ * lists (the next sf_fock_jk re-cuts them with the new bounds, splits or
+ * partition), so after any of them one more allocating sf_fock_jk call with
+ * the same arguments must come before the next sf_fock_jk_noalloc.  The
  * first call on a device looks up the device address of the static array
  * (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture.  Every call shares the one array: calls that overlap on
+ * any stream capture.  The address is kept for the life of the process: it
+ * assumes the device's primary context is never reset (cudaDeviceReset) while
+ * the library is loaded.  Every call shares the one array: calls that overlap on
  * the GPU (other streams, other threads, other handles) race and must be
  * serialised by the caller.  The array is cleared by each call before use. */
 #define SF_NOALLOC_MAX_NAO 1024

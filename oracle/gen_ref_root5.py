@@ -15,6 +15,9 @@ The oracle uses the library to pin its own root generator and, when present,
 as the root provider of the timed CPU baseline (the reference's arithmetic).
 
 Usage: python oracle/gen_ref_root5.py [path/to/core.f90]
+(default: $SEGFAULT_PY_REFERENCE/src/hf/core/core.f90).  Where the reference
+source is absent but oracle/_ref/ref_root5.c was transcribed earlier (and
+copied along with the working tree), only the compile step runs.
 """
 import os
 import re
@@ -23,7 +26,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_SRC = "/root/reference/src/hf/core/core.f90"
+# the reference checkout this recipe reads: $SEGFAULT_PY_REFERENCE, else its usual place here
+DEFAULT_SRC = os.path.join(os.environ.get("SEGFAULT_PY_REFERENCE", "/root/reference"), "src/hf/core/core.f90")
 
 
 def extract_root5(lines):
@@ -115,21 +119,32 @@ def transcribe(body):
     return "\n".join(head + params + decl + code + ["}"]) + "\n"
 
 
+def compile_c(cpath):
+    so = os.path.join(OUT, "librefroot5.so")
+    subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-o", so, cpath, "-lm"])
+    print("built", so)
+    return so
+
+
 def main(src=None):
     src = src or DEFAULT_SRC
+    cpath = os.path.join(OUT, "ref_root5.c")
     if not os.path.exists(src):
+        # a machine without the reference checkout: the transcription made
+        # where the source was (git-ignored, copied along with the working
+        # tree) is compiled for this machine's architecture
+        if os.path.exists(cpath):
+            compile_c(cpath)
+            return 0
         print("reference source not found: %s (oracle/_ref not built)" % src)
         return 1
     os.makedirs(OUT, exist_ok=True)
     with open(src) as f:
         body = extract_root5(f.read().split("\n"))
     c = transcribe(body)
-    cpath = os.path.join(OUT, "ref_root5.c")
     with open(cpath, "w") as f:
         f.write(c)
-    so = os.path.join(OUT, "librefroot5.so")
-    subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-o", so, cpath, "-lm"])
-    print("built", so)
+    compile_c(cpath)
     return 0
 
 

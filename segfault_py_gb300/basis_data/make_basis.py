@@ -17,7 +17,8 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = "/root/reference/src/hf/data/basis"
+# the reference checkout this script reads: $SEGFAULT_PY_REFERENCE, else its usual place here
+SRC = os.path.join(os.environ.get("SEGFAULT_PY_REFERENCE", "/root/reference"), "src/hf/data/basis")
 D_EXP = {"C": 0.8, "N": 0.8, "O": 0.8}
 P_EXP_H = 1.1
 

@@ -1353,8 +1353,8 @@ int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int3
     return fail(SF_ESTATE,
                 "sf_fock_jk_noalloc: the quartet lists for this precision and these cutoffs are not built; "
                 "call sf_fock_jk once with the same arguments first (that call allocates)");
-  DeviceGuard g(h->device);
   if (h->device < 0 || h->device >= 128) return fail(SF_EINVAL, "sf_fock_jk_noalloc: device index out of range");
+  DeviceGuard g(h->device);
   double *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);

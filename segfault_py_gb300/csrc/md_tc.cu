@@ -284,7 +284,20 @@ __global__ void __launch_bounds__(kTcThreads) md_tc_kernel(KParams kp, EriWork w
       __syncthreads();
       failed = *abort_flag != 0;
     }
-    if (failed) break;
+    if (failed) {
+      // the commit that timed out may still have MMAs writing the tensor
+      // memory: wait once more (bounded) for that phase before the memory is
+      // freed below; if it never completes the flag says so (the results of
+      // the whole launch are discarded by the host either way)
+      if (tid == 0) {
+        int it2 = 0;
+        while (!mbar_try_wait(mbar, phase ^ 1u) && ++it2 < kMaxWait) {
+        }
+        if (it2 >= kMaxWait && kp.err) atomicExch(kp.err, 3);
+      }
+      __syncthreads();
+      break;
+    }
     // accumulator rows (ab) -> output; warp w holds lanes 32w .. 32w+31
     tc_fence_after();
     float dv[kTcN];

@@ -86,12 +86,36 @@ def main(argv=None):
     ap.add_argument("--autotune", action="store_true", help="autotune the launch shapes first")
     ap.add_argument("--grad", action="store_true",
                     help="profile the two-electron gradient (sf_grad_jk) instead of the Fock build")
+    ap.add_argument("--one-electron", action="store_true",
+                    help="only the one-electron kernels: S, T, V (sf_one_electron) and their gradient "
+                         "(sf_grad_one_electron), --builds times each")
     a = ap.parse_args(argv)
     preload_torch_linalg()
     sym, xyz = geometry.water_cluster(a.nwater)
     mol = Molecule.from_geometry(sym, xyz, a.basis)
     fb = FockBuilder(mol, cutoff=a.cutoff, fp32_cutoff=a.fp32_cutoff, precision=a.precision)
     D = guess_density(fb, mol.nelectron // 2)
+    if a.one_electron:
+        from . import _lib
+        from .fock import _ptr, _stream_ptr
+        xyz, Z = mol.atom_table()
+        xyz_d = torch.as_tensor(xyz, device=fb.device)
+        Z_d = torch.as_tensor(Z, device=fb.device)
+        g = torch.zeros(3 * mol.natom, dtype=torch.float64, device=fb.device)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        for _ in range(a.builds):
+            fb.one_electron()
+        ev[1].record()
+        for _ in range(a.builds):
+            _lib.check(_lib.lib().sf_grad_one_electron(fb.handle, _ptr(xyz_d), _ptr(Z_d), mol.natom, _ptr(D),
+                                                       _ptr(D), _ptr(g), _stream_ptr()))
+        ev[2].record()
+        torch.cuda.synchronize()
+        print("== one-electron nao=%d natom=%d: S,T,V %.4f ms, gradient %.4f ms (mean of %d)"
+              % (fb.nao, mol.natom, ev[0].elapsed_time(ev[1]) / a.builds, ev[1].elapsed_time(ev[2]) / a.builds,
+                 a.builds))
+        return
     if a.autotune:
         tab = fb.autotune(D, reps=3)
         gain = sum(e["ms_default"] - e["ms_tuned"] for e in tab)

@@ -175,7 +175,9 @@ def ccpvdz_recorded(ref):
                 note="recorded = src/hf/benchmark/molecule_test.json (reference energy etot, psi4 energy, wall s)")
 
 
-def main(ref="/root/reference"):
+def main(ref=None):
+    # the reference checkout this script reads: argument, $SEGFAULT_PY_REFERENCE, else its usual place here
+    ref = ref or os.environ.get("SEGFAULT_PY_REFERENCE", "/root/reference")
     import tempfile
     sys.path.insert(0, os.path.join(ref, "src/hf"))
     sys.path.insert(0, REPO)

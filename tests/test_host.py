@@ -200,5 +200,23 @@ def test_bench_dominant_kernel_sums_launches_of_one_kernel():
     slices = [sl((2, 0, 1, 1), 2, 0.05), sl((1, 0, 0, 0), 1, 0.03), sl((1, 0, 0, 0), 1, 0.04),
               sl((1, 0, 0, 0), 2, 0.02)]
     top, group, name = bench.dominant_kernel(slices)
-    assert name == "jk_kernel<1,0,0,0,fp32>" and name in bench.NCU_TRAFFIC
+    assert name == "jk_kernel<1,0,0,0,fp32>"
     assert len(group) == 2 and top["ms"] == 0.04
+
+
+def test_bench_traffic_table_is_keyed_to_the_kernel_sources(tmp_path):
+    """The committed ncu traffic table is used only for the kernel sources it
+    was measured on: a table with another source hash gives traffic = null."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", f"{REPO}/bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    t = tmp_path / "traffic.txt"
+    t.write_text("# csrc_sha16 %s\njk_kernel<1,0,0,0,fp32> 1234\n" % bench.csrc_hash())
+    bench.TRAFFIC_TABLE = str(t)
+    v, src = bench.ncu_traffic("jk_kernel<1,0,0,0,fp32>")
+    assert v == 1234.0 and "ncu capture" in src
+    assert bench.ncu_traffic("jk_kernel<2,0,0,0,dd>")[0] is None
+    t.write_text("# csrc_sha16 0000000000000000\njk_kernel<1,0,0,0,fp32> 1234\n")
+    v, src = bench.ncu_traffic("jk_kernel<1,0,0,0,fp32>")
+    assert v is None and "stale" in src

@@ -76,3 +76,31 @@ def test_noalloc_rejects_unprepared_and_oversized(cuda):
     assert L.sf_fock_jk_noalloc(fb.handle, _ptr(D), _ptr(D), _ptr(D), 0, 1e-12, 1e-5, st) == -1
     assert b"SF_NOALLOC_MAX_NAO" in L.sf_last_error()
     fb.close()
+
+
+def test_noalloc_needs_fresh_lists_after_retuning(cuda):
+    """sf_autotune re-cuts the quartet lists: the allocation-free call then
+    refuses (SF_ESTATE) until one allocating sf_fock_jk has rebuilt them."""
+    from segfault_py_gb300 import _lib, geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.molecule import Molecule
+    L = _lib.lib()
+    s, x = G.water_cluster(2, seed=5)
+    mol = Molecule.from_geometry(s, x, "6-31g*")
+    n = mol.nao
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((n, n)) * 0.05
+    D = torch.tensor(A + A.T, device=cuda)
+    fb = FockBuilder(mol, device=cuda, cutoff=1e-12, fp32_cutoff=1e-5)
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    J = torch.empty_like(D)
+    K = torch.empty_like(D)
+    fb.autotune(D, precision="fp64", reps=1)
+    assert L.sf_fock_jk_noalloc(fb.handle, _ptr(D), _ptr(J), _ptr(K), 0, 1e-12, 1e-5, st) == -4
+    Jr, Kr = fb.jk(D, precision="fp64")
+    assert L.sf_fock_jk_noalloc(fb.handle, _ptr(D), _ptr(J), _ptr(K), 0, 1e-12, 1e-5, st) == 0, L.sf_last_error()
+    torch.cuda.synchronize()
+    scale = max(float(Jr.abs().max()), float(Kr.abs().max()))
+    assert float((J - Jr).abs().max()) <= 1e-12 * scale
+    assert float((K - Kr).abs().max()) <= 1e-12 * scale
+    fb.close()
