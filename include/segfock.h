@@ -165,6 +165,25 @@ int32_t sf_tuning_count(const sf_handle *h);
 int sf_get_tuning(const sf_handle *h, int32_t idx, sf_tune_entry *out);
 int sf_set_tuning(sf_handle *h, const sf_tune_entry *entries, int32_t n);
 
+/* Density-weighted classification of the quartet lists, redone on the device
+ * by every sf_fock_jk / sf_grad_jk call from its density D (no counterpart in
+ * the reference, which computes every quartet in FP64).  With M_xy the
+ * largest |D| element of the block of shells x, y:
+ *  - Fock build, mixed modes: a quartet of the accurate tier (Q_ab Q_cd >=
+ *    fp32_cutoff) stays there only while Q_ab Q_cd max(2M_ab, 2M_cd, M_ac,
+ *    M_bd, M_ad, M_bc) -- a bound on what it adds to any element of J or K --
+ *    is >= fock_fp32_cutoff; otherwise it runs in FP32;
+ *  - gradient: a quartet whose Q_ab Q_cd (M_ab M_cd/2 + (M_ac M_bd +
+ *    M_ad M_bc)/8) is below grad_drop_cutoff is left out; in the mixed modes
+ *    one of the accurate tier with that bound below grad_fp32_cutoff runs in
+ *    FP32.
+ * A negative cutoff means the call's own: fp32_cutoff for the two FP32
+ * cutoffs, the Schwarz cutoff for the drop cutoff.  on = 0 turns the
+ * classification off (every call then uses the Schwarz-sorted lists as cut).
+ * Default: on, all three cutoffs negative. */
+int sf_set_density_screening(sf_handle *h, int32_t on, double fock_fp32_cutoff, double grad_drop_cutoff,
+                             double grad_fp32_cutoff);
+
 /* Restrict sf_fock_jk to the slice [part, part+1) of nparts equal-work slices
  * of every quartet class (replica / multi-GPU partitioning hook; 0,1 = all). */
 int sf_set_partition(sf_handle *h, int32_t part, int32_t nparts);

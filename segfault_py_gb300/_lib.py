@@ -23,7 +23,8 @@ EXPORTS = ["sf_version", "sf_last_error", "sf_create", "sf_build_shells", "sf_de
            "sf_schwarz", "sf_fock_jk", "sf_set_partition", "sf_eri_batch", "sf_one_electron", "sf_rys_roots_host", "sf_set_profiling", "sf_slice_count", "sf_get_slice_info",
            "sf_fma_peak", "sf_fock_jk_noalloc", "sf_grad_jk", "sf_grad_one_electron",
            "sf_small_solve", "sf_eri_plan_create", "sf_eri_plan_info", "sf_eri_plan_offsets", "sf_eri_plan_run",
-           "sf_eri_plan_destroy", "sf_autotune", "sf_tuning_count", "sf_get_tuning", "sf_set_tuning", "sf_eri_plan_run_md"]
+           "sf_eri_plan_destroy", "sf_autotune", "sf_tuning_count", "sf_get_tuning", "sf_set_tuning", "sf_eri_plan_run_md",
+           "sf_set_density_screening"]
 
 
 class SegFockUnavailable(ImportError):
@@ -120,6 +121,7 @@ def lib():
     L.sf_tuning_count.restype = i32
     L.sf_get_tuning.argtypes = [p, i32, p]
     L.sf_set_tuning.argtypes = [p, p, i32]
+    L.sf_set_density_screening.argtypes = [p, i32, d, d, d]
     _lib = L
     return L
 

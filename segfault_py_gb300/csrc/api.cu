@@ -165,6 +165,117 @@ __global__ void to_dd_kernel(const double *D, float2 *Dd, int64_t n) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Density-weighted classification of the quartet lists, on the device, once
+// per Fock build or gradient (the density changes between calls).  With M_xy
+// the largest |D| element of the shell block (x, y):
+//  * Fock build: a quartet adds at most Q_ab Q_cd * max(2 M_ab, 2 M_cd, M_ac,
+//    M_bd, M_ad, M_bc) to any element of J or K (the eight index
+//    permutations of hf.py:49-60); the mixed modes keep a quartet of the
+//    accurate tier (Q_ab Q_cd >= fp32 cutoff) there only while this bound is
+//    >= its cutoff, else it runs in FP32 (demoted);
+//  * gradient: every contraction coefficient is bounded by
+//    G = M_ab M_cd / 2 + (M_ac M_bd + M_ad M_bc) / 8, so a quartet whose
+//    Q_ab Q_cd G is below the drop cutoff is left out (density screening) and
+//    one of the accurate tier with Q_ab Q_cd G below the accurate cutoff runs
+//    in FP32.
+// Every list is compacted into a "kept" and a "demoted" list at the same
+// offsets (d_keep, d_dem), order kept within each chunk of 1024 entries, with
+// device counts read by the kernels, so nothing synchronises with the host.
+struct ClassifySlice {
+  int64_t off, n;        // offset in the quartet-list buffer, length
+  int x0, y0;            // first global pair of the bra / ket pair class
+  int acc;               // accurate tier (FP64 or double-float launch)
+  int pad;
+};
+constexpr int kClsThreads = 256, kClsPer = 4, kClsChunk = kClsThreads * kClsPer;
+
+// M_xy = max |D| over the Cartesian block of shells x, y (FP32 is enough for a bound)
+__global__ void shell_dmax_kernel(const double *D, int n, const int *l, const int *ao, int ns, float *dm) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= ns * ns) return;
+  const int a = idx / ns, b = idx % ns;
+  const int la = l[a], lb = l[b], a0 = ao[a], b0 = ao[b];
+  const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2;
+  double m = 0.0;
+  for (int i = 0; i < na; ++i)
+    for (int j = 0; j < nb; ++j) m = fmax(m, fabs(D[(int64_t)(a0 + i) * n + b0 + j]));
+  dm[idx] = (float)m;
+}
+
+__global__ void __launch_bounds__(kClsThreads) classify_kernel(
+    const int2 *list, const ClassifySlice *sl, const int2 *blk, const int *pa, const int *pb, const int *pnp,
+    const double *pq, const float *dm, int ns, int grad_mode, double t_drop, double t_acc, int2 *keep, int2 *dem,
+    unsigned long long *cnt) {
+  const int2 bk = blk[blockIdx.x];
+  const ClassifySlice S = sl[bk.x];
+  const int64_t e0 = (int64_t)bk.y * kClsChunk + (int64_t)threadIdx.x * kClsPer;
+  int2 v[kClsPer];
+  int where[kClsPer];   // 0 kept, 1 demoted, 2 left out
+  int nk = 0, nd = 0;
+  unsigned long long pk = 0, pd = 0;
+#pragma unroll
+  for (int k = 0; k < kClsPer; ++k) {
+    where[k] = 2;
+    const int64_t e = e0 + k;
+    if (e >= S.n) continue;
+    v[k] = list[S.off + e];
+    const int pab = S.x0 + v[k].x, pcd = S.y0 + v[k].y;
+    const int a = pa[pab], b = pb[pab], c = pa[pcd], d = pb[pcd];
+    const float mab = dm[a * ns + b], mcd = dm[c * ns + d], mac = dm[a * ns + c], mbd = dm[b * ns + d],
+                mad = dm[a * ns + d], mbc = dm[b * ns + c];
+    const double q = pq[pab] * pq[pcd];
+    double bound;
+    if (grad_mode) bound = q * (double)(0.5f * mab * mcd + 0.125f * (mac * mbd + mad * mbc));
+    else bound = q * (double)fmaxf(2.0f * fmaxf(mab, mcd), fmaxf(fmaxf(mac, mbd), fmaxf(mad, mbc)));
+    where[k] = bound < t_drop ? 2 : (S.acc && bound < t_acc) ? 1 : 0;
+    const unsigned long long c0 = (unsigned long long)pnp[pab] * (unsigned long long)pnp[pcd];
+    if (where[k] == 0) { ++nk; pk += c0; }
+    if (where[k] == 1) { ++nd; pd += c0; }
+  }
+  // exclusive scan of (nk, nd) over the CTA: warp shuffles, then the warp totals
+  __shared__ int s_wk[kClsThreads / 32], s_wd[kClsThreads / 32];
+  __shared__ unsigned long long s_base[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int ik = nk, id = nd;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int tk = __shfl_up_sync(0xffffffffu, ik, off), td = __shfl_up_sync(0xffffffffu, id, off);
+    if (lane >= off) { ik += tk; id += td; }
+  }
+  unsigned long long sk = pk, sd = pd;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    sk += __shfl_xor_sync(0xffffffffu, sk, off);
+    sd += __shfl_xor_sync(0xffffffffu, sd, off);
+  }
+  if (lane == 31) { s_wk[warp] = ik; s_wd[warp] = id; }
+  if (lane == 0) {
+    if (sk) atomicAdd(cnt + 4 * bk.x + 2, sk);
+    if (sd) atomicAdd(cnt + 4 * bk.x + 3, sd);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tk = 0, td = 0;
+    for (int w = 0; w < kClsThreads / 32; ++w) {
+      const int a = s_wk[w], b = s_wd[w];
+      s_wk[w] = tk;
+      s_wd[w] = td;
+      tk += a;
+      td += b;
+    }
+    s_base[0] = tk ? atomicAdd(cnt + 4 * bk.x, (unsigned long long)tk) : 0ull;
+    s_base[1] = td ? atomicAdd(cnt + 4 * bk.x + 1, (unsigned long long)td) : 0ull;
+  }
+  __syncthreads();
+  int64_t ok = (int64_t)s_base[0] + s_wk[warp] + ik - nk, od = (int64_t)s_base[1] + s_wd[warp] + id - nd;
+#pragma unroll
+  for (int k = 0; k < kClsPer; ++k) {
+    if (where[k] == 0) keep[S.off + ok++] = v[k];
+    else if (where[k] == 1) dem[S.off + od++] = v[k];
+  }
+}
+
 }  // namespace
 
 struct sf_handle {
@@ -232,6 +343,25 @@ struct sf_handle {
   // fill target of the accurate tier of a mixed mode (-1: fill_x4 of the mode)
   int fill_acc_x4[5] = {-1, -1, -1, -1, -1};
   KParams kp;
+  // density-weighted classification (see classify_kernel); cutoffs < 0 mean
+  // the call's own: fp32_cutoff for the accurate tiers, the Schwarz cutoff
+  // for the gradient's drop bound
+  int dens_on = 1;
+  double dens_fock_acc = -1.0, dens_grad_drop = -1.0, dens_grad_acc = -1.0;
+  DBuf<float> d_dmax;                      // nshell^2 block maxima of |D|
+  DBuf<int2> d_keep, d_dem;                // compacted lists at the offsets of d_list
+  DBuf<unsigned long long> d_cnt;          // per slice: kept, demoted quartets; kept, demoted primitive quartets
+  DBuf<ClassifySlice> d_csl;
+  DBuf<int2> d_blk_acc, d_blk_all;         // classification CTAs (slice, chunk): accurate-tier slices / all
+  int nblk_acc = 0, nblk_all = 0;
+  // the launches of the last Fock build or gradient: one per slice, plus one
+  // FP32 launch per accurate-tier slice for its demoted quartets
+  struct Launch {
+    int slice, kind, stream, demoted;
+    ClassWork w;
+  };
+  std::vector<Launch> plan;
+  bool plan_counts = false;                // quartet counts of the plan live on the device
 };
 
 namespace {
@@ -483,6 +613,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     w.same = p.same;
     w.psplit = p.psplit;
     w.wsplit = p.wsplit;
+    w.max_cost = (int)std::max<int64_t>(p.cost_hi, 1);
     h->slices.push_back({p.cls, p.prec, w, p.n, p.prims, p.flops, p.cost_hi});
   }
   // greedy longest-processing-time assignment of slices to side streams;
@@ -536,12 +667,104 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       h->slice_stream = lpt_streams(cost);
     }
   }
+  // tables of the density-weighted classification
+  {
+    std::vector<ClassifySlice> csl(h->slices.size());
+    std::vector<int2> ba, bl;
+    for (size_t k = 0; k < h->slices.size(); ++k) {
+      const auto &sl = h->slices[k];
+      csl[k] = ClassifySlice{(int64_t)(sl.w.list - h->d_list.p), sl.w.n, sl.w.x0, sl.w.y0, sl.prec != 1 ? 1 : 0, 0};
+      for (int64_t c = 0; c * kClsChunk < sl.w.n; ++c) {
+        bl.push_back(make_int2((int)k, (int)c));
+        if (sl.prec != 1) ba.push_back(make_int2((int)k, (int)c));
+      }
+    }
+    SF_CK(h->d_csl.upload(csl));
+    SF_CK(h->d_blk_acc.upload(ba));
+    SF_CK(h->d_blk_all.upload(bl));
+    h->nblk_acc = (int)ba.size();
+    h->nblk_all = (int)bl.size();
+    SF_CK(h->d_keep.alloc(all.size()));
+    SF_CK(h->d_dem.alloc(all.size()));
+    SF_CK(h->d_cnt.alloc(4 * std::max<size_t>(h->slices.size(), 1)));
+    SF_CK(h->d_dmax.alloc((size_t)h->nshell * h->nshell));
+  }
   h->c_prec = prec;
   h->c_cut = cut;
   h->c_cut32 = cut32;
   h->c_part = h->part;
   h->c_nparts = h->nparts;
   return SF_OK;
+}
+
+// Classify the current lists against the density D (see classify_kernel):
+// for a Fock build only in the mixed modes (demotion of the accurate tier),
+// for a gradient always (drop bound; demotion too in the mixed modes).
+// Returns 1 when the launches must read the compacted lists, 0 when the
+// lists are used as they are.
+int density_classify(sf_handle *h, const double *D, bool grad, double cut, double cut32, cudaStream_t st,
+                     int *launches, int *active) {
+  *active = 0;
+  if (!h->dens_on || h->slices.empty()) return SF_OK;
+  bool has32 = false, hasacc = false;
+  for (const auto &sl : h->slices) (sl.prec == 1 ? has32 : hasacc) = true;
+  const bool mixed = has32 && hasacc;
+  if (!grad && !mixed) return SF_OK;
+  const double t_acc = mixed ? ((grad ? h->dens_grad_acc : h->dens_fock_acc) >= 0.0
+                                    ? (grad ? h->dens_grad_acc : h->dens_fock_acc)
+                                    : cut32)
+                             : -1.0;
+  const double t_drop = grad ? (h->dens_grad_drop >= 0.0 ? h->dens_grad_drop : cut) : -1.0;
+  const int nb = grad ? h->nblk_all : h->nblk_acc;
+  const int ns = h->nshell;
+  SF_CK(cudaMemsetAsync(h->d_cnt.p, 0, 4 * h->slices.size() * sizeof(unsigned long long), st));
+  shell_dmax_kernel<<<(unsigned)((ns * ns + 255) / 256), 256, 0, st>>>(D, h->nao, h->d_l.p, h->d_ao.p, ns,
+                                                                       h->d_dmax.p);
+  SF_CK(cudaGetLastError());
+  if (nb > 0) {
+    classify_kernel<<<(unsigned)nb, kClsThreads, 0, st>>>(
+        h->d_list.p, h->d_csl.p, grad ? h->d_blk_all.p : h->d_blk_acc.p, h->d_pa.p, h->d_pb.p, h->d_pnp.p, h->d_pq.p,
+        h->d_dmax.p, ns, grad ? 1 : 0, t_drop, t_acc, h->d_keep.p, h->d_dem.p, h->d_cnt.p);
+    SF_CK(cudaGetLastError());
+  }
+  if (launches) *launches += nb > 0 ? 2 : 1;
+  *active = 1;
+  return SF_OK;
+}
+
+// The launches of one call: one per slice (reading its compacted list when
+// the classification ran for it) and, for a classified accurate-tier slice of
+// a mixed mode, one FP32 launch of its demoted quartets on the next FP32
+// stream.
+void make_plan(sf_handle *h, bool grad, int active) {
+  h->plan.clear();
+  h->plan_counts = active != 0;
+  bool has32 = false, hasacc = false;
+  for (const auto &sl : h->slices) (sl.prec == 1 ? has32 : hasacc) = true;
+  const bool mixed = has32 && hasacc;
+  int rr = 0;
+  for (size_t k = 0; k < h->slices.size(); ++k) {
+    const auto &sl = h->slices[k];
+    const bool cl = active && (grad || sl.prec != 1);
+    const int64_t off = sl.w.list - h->d_list.p;
+    sf_handle::Launch L{(int)k, sl.prec, h->slice_stream[k], 0, sl.w};
+    if (cl) {
+      L.w.list = h->d_keep.p + off;
+      L.w.count = h->d_cnt.p + 4 * k;
+    }
+    h->plan.push_back(L);
+    if (cl && mixed && sl.prec != 1) {
+      sf_handle::Launch Dm{(int)k, 1, sf_handle::kHiStreams + rr, 1, sl.w};
+      rr = (rr + 1) % (sf_handle::kSideStreams - sf_handle::kHiStreams);
+      Dm.w.list = h->d_dem.p + off;
+      Dm.w.count = h->d_cnt.p + 4 * k + 1;
+      const int S = std::max(1, sl.w.psplit) * std::max(1, sl.w.wsplit);
+      const int pmax = 32 / kClassInfo[sl.cls].t32;
+      Dm.w.psplit = std::min(S, pmax);
+      Dm.w.wsplit = std::max(1, std::min(S / Dm.w.psplit, kMaxWsplit));
+      h->plan.push_back(Dm);
+    }
+  }
 }
 
 // Run fn(k, stream) for every slice k on its side stream (forked from st,
@@ -562,10 +785,6 @@ int fan_out_list(sf_handle *h, cudaStream_t st, const std::vector<int> &stream_o
   return SF_OK;
 }
 
-template <typename F>
-int fan_out(sf_handle *h, cudaStream_t st, F &&fn) {
-  return fan_out_list(h, st, h->slice_stream, fn);
-}
 
 
 // one launch of the current quartet lists, in its kind's arithmetic
@@ -576,16 +795,33 @@ cudaError_t launch_slice(sf_handle *h, const sf_handle::Slice &s, const ClassWor
   return launch_jk_dd(s.cls, h->kp, w, reinterpret_cast<const dd *>(h->d_Ddd.p), Jh, Kh, st);
 }
 
-// Launch every slice of the current quartet lists on the side streams
-// (forked from st, joined back into st).  Events of the profiling mode
-// bracket each launch on its own stream.
-int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, double *Kh, cudaStream_t st,
-                  int profiling, int *launches) {
-  if (profiling == 2) {   // serialised on the caller's stream
-    for (size_t k = 0; k < h->slices.size(); ++k) {
-      const auto &s = h->slices[k];
+int profiling_events(sf_handle *h, cudaStream_t st);
+
+// one launch of the plan: J/K digestion (Jh, Kh) or gradient (g) kernels in
+// the launch's arithmetic
+cudaError_t launch_one(sf_handle *h, const sf_handle::Launch &L, bool grad, const double *D, const float *D32,
+                       double *Jh, double *Kh, double *g, cudaStream_t st) {
+  const int cls = h->slices[L.slice].cls;
+  const dd *Ddd = reinterpret_cast<const dd *>(h->d_Ddd.p);
+  if (grad) {
+    if (L.kind == 0) return launch_grad_f64(cls, h->kp, L.w, D, g, st);
+    if (L.kind == 1) return launch_grad_f32(cls, h->kp, L.w, D32, g, st);
+    return launch_grad_dd(cls, h->kp, L.w, Ddd, g, st);
+  }
+  if (L.kind == 0) return launch_jk_f64(cls, h->kp, L.w, D, Jh, Kh, st);
+  if (L.kind == 1) return launch_jk_f32(cls, h->kp, L.w, D32, Jh, Kh, st);
+  return launch_jk_dd(cls, h->kp, L.w, Ddd, Jh, Kh, st);
+}
+
+// Run every launch of the plan on its side stream (forked from st, joined
+// back into st); profiling 1: events bracket each launch on its own stream;
+// profiling 2: the launches are serialised on st, each between two events.
+int run_plan(sf_handle *h, bool grad, const double *D, const float *D32, double *Jh, double *Kh, double *g,
+             cudaStream_t st, int profiling, int *launches) {
+  if (profiling == 2) {
+    for (size_t k = 0; k < h->plan.size(); ++k) {
       SF_CK(cudaEventRecord(h->ev[2 * k], st));
-      SF_CK(launch_slice(h, s, s.w, D, D32, Jh, Kh, st));
+      SF_CK(launch_one(h, h->plan[k], grad, D, D32, Jh, Kh, g, st));
       SF_CK(cudaEventRecord(h->ev[2 * k + 1], st));
       if (launches) ++*launches;
     }
@@ -593,14 +829,14 @@ int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, d
   }
   SF_CK(cudaEventRecord(h->fork_ev, st));
   bool used[sf_handle::kSideStreams] = {false};
-  for (size_t k = 0; k < h->slices.size(); ++k) used[h->slice_stream[k]] = true;
+  for (const auto &L : h->plan) used[L.stream] = true;
   for (int j = 0; j < sf_handle::kSideStreams; ++j)
     if (used[j]) SF_CK(cudaStreamWaitEvent(h->side[j], h->fork_ev, 0));
-  for (size_t k = 0; k < h->slices.size(); ++k) {
-    const auto &s = h->slices[k];
-    cudaStream_t ss = h->side[h->slice_stream[k]];
+  for (size_t k = 0; k < h->plan.size(); ++k) {
+    const auto &L = h->plan[k];
+    cudaStream_t ss = h->side[L.stream];
     if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k], ss));
-    SF_CK(launch_slice(h, s, s.w, D, D32, Jh, Kh, ss));
+    SF_CK(launch_one(h, L, grad, D, D32, Jh, Kh, g, ss));
     if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k + 1], ss));
     if (launches) ++*launches;
   }
@@ -612,10 +848,24 @@ int launch_slices(sf_handle *h, const double *D, const float *D32, double *Jh, d
   return SF_OK;
 }
 
+// classification, plan and launches of one Fock build (Jh, Kh) or gradient (g)
+int run_call(sf_handle *h, bool grad, const double *D, const float *D32, double *Jh, double *Kh, double *g,
+             double cut, double cut32, cudaStream_t st, int profiling, int *launches) {
+  int active = 0;
+  int rc = density_classify(h, D, grad, cut, cut32, st, launches, &active);
+  if (rc) return rc;
+  make_plan(h, grad, active);
+  if (profiling) {
+    rc = profiling_events(h, st);
+    if (rc) return rc;
+  }
+  return run_plan(h, grad, D, D32, Jh, Kh, g, st, profiling, launches);
+}
+
 // events of the profiling modes: two per launch plus the build's start,
 // recorded on the caller's stream before the launches fork
 int profiling_events(sf_handle *h, cudaStream_t st) {
-  while (h->ev.size() < 2 * h->slices.size()) {
+  while (h->ev.size() < 2 * h->plan.size()) {
     cudaEvent_t e;
     SF_CK(cudaEventCreate(&e));
     h->ev.push_back(e);
@@ -644,6 +894,50 @@ int convert_density(sf_handle *h, const double *D, float *D32, cudaStream_t st, 
     SF_CK(cudaGetLastError());
     if (launches) ++*launches;
   }
+  return SF_OK;
+}
+
+// work counters of the last plan: the host counts of the lists, or, when the
+// lists were classified on the device, the device counts (the stream must be
+// synchronised)
+int plan_stats(sf_handle *h, sf_stats *stats) {
+  stats->quartets_total = h->st_total;
+  stats->reserved = 0;
+  if (!h->plan_counts) {
+    stats->quartets_fp64 = h->st_q[0];
+    stats->quartets_fp32 = h->st_q[1];
+    stats->prim_quartets_fp64 = h->st_pq[0];
+    stats->prim_quartets_fp32 = h->st_pq[1];
+    stats->flop_alg_fp64 = h->st_f[0];
+    stats->flop_alg_fp32 = h->st_f[1];
+    return SF_OK;
+  }
+  std::vector<unsigned long long> c(4 * h->slices.size());
+  SF_CK(cudaMemcpy(c.data(), h->d_cnt.p, c.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  int64_t q[2] = {0, 0}, pq[2] = {0, 0};
+  double f[2] = {0.0, 0.0};
+  for (const auto &L : h->plan) {
+    const auto &sl = h->slices[L.slice];
+    const ClassInfo &ci = kClassInfo[sl.cls];
+    const double nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
+    const double nabcd = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
+    int64_t nq = sl.quartets, np = sl.prims;
+    if (L.w.count) {
+      const size_t o = 4 * (size_t)L.slice + (L.demoted ? 1 : 0);
+      nq = (int64_t)c[o];
+      np = (int64_t)c[o + 2];
+    }
+    const int t = L.kind == 1 ? 1 : 0;
+    q[t] += nq;
+    pq[t] += np;
+    f[t] += (double)np * nr * 4.0 * nabcd + 12.0 * nabcd * (double)nq;
+  }
+  stats->quartets_fp64 = q[0];
+  stats->quartets_fp32 = q[1];
+  stats->prim_quartets_fp64 = pq[0];
+  stats->prim_quartets_fp32 = pq[1];
+  stats->flop_alg_fp64 = f[0];
+  stats->flop_alg_fp32 = f[1];
   return SF_OK;
 }
 
@@ -995,24 +1289,46 @@ int sf_set_profiling(sf_handle *h, int32_t on) {
   return SF_OK;
 }
 
-int32_t sf_slice_count(const sf_handle *h) { return h ? (int32_t)h->slices.size() : -1; }
+int32_t sf_slice_count(const sf_handle *h) {
+  return h ? (int32_t)(h->plan.empty() ? h->slices.size() : h->plan.size()) : -1;
+}
 
 int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out) {
-  if (!h || !out || idx < 0 || idx >= (int32_t)h->slices.size()) return fail(SF_EINVAL, "sf_get_slice_info: bad index");
+  if (!h || !out || idx < 0 || idx >= sf_slice_count(h)) return fail(SF_EINVAL, "sf_get_slice_info: bad index");
   DeviceGuard g(h->device);
-  const auto &s = h->slices[idx];
+  // a launch of the last call's plan (before any call: the slices themselves)
+  sf_handle::Launch L{idx, 0, 0, 0, ClassWork{}};
+  if (h->plan.empty()) {
+    L.kind = h->slices[idx].prec;
+    L.stream = (size_t)idx < h->slice_stream.size() ? h->slice_stream[idx] : -1;
+    L.w = h->slices[idx].w;
+  } else {
+    L = h->plan[idx];
+  }
+  const auto &s = h->slices[L.slice];
   const ClassInfo &ci = kClassInfo[s.cls];
   out->cls = s.cls;
-  out->precision = s.prec;
+  out->precision = L.kind;
   out->la = ci.la; out->lb = ci.lb; out->lc = ci.lc; out->ld = ci.ld;
   out->quartets = s.quartets;
   out->prim_quartets = s.prims;
   out->flop_alg = s.flops;
-  out->threads_per_quartet = (s.prec == 1 ? ci.t32 : ci.t64) * s.w.psplit * s.w.wsplit;
+  if (L.w.count) {   // classified on the device: its counts
+    unsigned long long c[2] = {0, 0};
+    SF_CK(cudaDeviceSynchronize());
+    SF_CK(cudaMemcpy(&c[0], L.w.count, sizeof(c[0]), cudaMemcpyDeviceToHost));
+    SF_CK(cudaMemcpy(&c[1], L.w.count + 2, sizeof(c[1]), cudaMemcpyDeviceToHost));
+    const double nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
+    const double nabcd = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
+    out->quartets = (int64_t)c[0];
+    out->prim_quartets = (int64_t)c[1];
+    out->flop_alg = (double)c[1] * nr * 4.0 * nabcd + 12.0 * nabcd * (double)c[0];
+  }
+  out->threads_per_quartet = (L.kind == 1 ? ci.t32 : ci.t64) * L.w.psplit * L.w.wsplit;
   out->ms = -1.0f;
   out->start_ms = -1.0f;
-  out->stream = (h->profiling == 2 || (size_t)idx >= h->slice_stream.size()) ? -1 : h->slice_stream[idx];
-  if (h->profiling && h->ev.size() >= 2 * h->slices.size()) {
+  out->stream = h->profiling == 2 ? -1 : L.stream;
+  if (h->profiling && h->ev.size() >= 2 * (size_t)sf_slice_count(h)) {
     SF_CK(cudaEventSynchronize(h->ev[2 * idx + 1]));
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, h->ev[2 * idx], h->ev[2 * idx + 1]) == cudaSuccess) out->ms = ms;
@@ -1073,6 +1389,18 @@ int sf_schwarz(sf_handle *h, double *q_out, void *stream) {
   return SF_OK;
 }
 
+int sf_set_density_screening(sf_handle *h, int32_t on, double fock_fp32_cutoff, double grad_drop_cutoff,
+                             double grad_fp32_cutoff) {
+  if (!h) return fail(SF_EINVAL, "sf_set_density_screening: NULL handle");
+  if (std::isnan(fock_fp32_cutoff) || std::isnan(grad_drop_cutoff) || std::isnan(grad_fp32_cutoff))
+    return fail(SF_EINVAL, "sf_set_density_screening: NaN cutoff");
+  h->dens_on = on ? 1 : 0;
+  h->dens_fock_acc = fock_fp32_cutoff;
+  h->dens_grad_drop = grad_drop_cutoff;
+  h->dens_grad_acc = grad_fp32_cutoff;
+  return SF_OK;
+}
+
 int sf_set_partition(sf_handle *h, int32_t part, int32_t nparts) {
   if (!h || nparts < 1 || part < 0 || part >= nparts) return fail(SF_EINVAL, "sf_set_partition: bad slice");
   h->part = part;
@@ -1098,26 +1426,17 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
   int launches = 0;
   rc = convert_density(h, D, h->d_D32.p, st, &launches);
   if (rc) return rc;
-  if (h->profiling) {
-    rc = profiling_events(h, st);
-    if (rc) return rc;
-  }
-  rc = launch_slices(h, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st, h->profiling, &launches);
+  rc = run_call(h, false, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, nullptr, cutoff, fp32_cutoff, st, h->profiling,
+                &launches);
   if (rc) return rc;
   symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(h->d_Jh.p, h->d_Kh.p, J, K, n);
   SF_CK(cudaGetLastError());
   ++launches;
   if (stats) {
-    stats->quartets_fp64 = h->st_q[0];
-    stats->quartets_fp32 = h->st_q[1];
-    stats->quartets_total = h->st_total;
-    stats->prim_quartets_fp64 = h->st_pq[0];
-    stats->prim_quartets_fp32 = h->st_pq[1];
-    stats->flop_alg_fp64 = h->st_f[0];
-    stats->flop_alg_fp32 = h->st_f[1];
-    stats->launches = launches;
-    stats->reserved = 0;
     SF_CK(cudaStreamSynchronize(st));
+    rc = plan_stats(h, stats);
+    if (rc) return rc;
+    stats->launches = launches;
   }
   return SF_OK;
 }
@@ -1161,11 +1480,12 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
   auto time_build = [&](float *ms) -> int {
     int r2 = build_work(h, precision, cutoff, fp32_cutoff);
     if (r2) return r2;
-    r2 = launch_slices(h, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st, 0, nullptr);   // warm-up
+    r2 = run_call(h, false, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, nullptr, cutoff, fp32_cutoff, st, 0,
+                  nullptr);   // warm-up
     if (r2) return r2;
     SF_CK(cudaEventRecord(e0, st));
     for (int r = 0; r < reps; ++r) {
-      r2 = launch_slices(h, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, st, 0, nullptr);
+      r2 = run_call(h, false, D, h->d_D32.p, h->d_Jh.p, h->d_Kh.p, nullptr, cutoff, fp32_cutoff, st, 0, nullptr);
       if (r2) return r2;
     }
     SF_CK(cudaEventRecord(e1, st));
@@ -1377,7 +1697,7 @@ int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int3
     to_float_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(D, D32, (int64_t)nn);
     SF_CK(cudaGetLastError());
   }
-  int rc = launch_slices(h, D, D32, Jh, Kh, st, 0, nullptr);
+  int rc = run_call(h, false, D, D32, Jh, Kh, nullptr, cutoff, fp32_cutoff, st, 0, nullptr);
   if (rc) return rc;
   symmetrize_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(Jh, Kh, J, K, n);
   SF_CK(cudaGetLastError());
@@ -1397,31 +1717,8 @@ int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, d
   if (rc) return rc;
   rc = convert_density(h, D, h->d_D32.p, st, nullptr);
   if (rc) return rc;
-  auto launch = [&](size_t k, cudaStream_t ss) {
-    const auto &s = h->slices[k];
-    if (s.prec == 0) return launch_grad_f64(s.cls, h->kp, s.w, D, grad, ss);
-    if (s.prec == 1) return launch_grad_f32(s.cls, h->kp, s.w, h->d_D32.p, grad, ss);
-    return launch_grad_dd(s.cls, h->kp, s.w, reinterpret_cast<const dd *>(h->d_Ddd.p), grad, ss);
-  };
-  if (h->profiling) {   // per-launch events (serialised in mode 2), read by sf_get_slice_info
-    const int rc = profiling_events(h, st);
-    if (rc) return rc;
-    if (h->profiling == 2) {
-      for (size_t k = 0; k < h->slices.size(); ++k) {
-        SF_CK(cudaEventRecord(h->ev[2 * k], st));
-        SF_CK(launch(k, st));
-        SF_CK(cudaEventRecord(h->ev[2 * k + 1], st));
-      }
-      return SF_OK;
-    }
-    return fan_out(h, st, [&](size_t k, cudaStream_t ss) {
-      cudaError_t e = cudaEventRecord(h->ev[2 * k], ss);
-      if (e == cudaSuccess) e = launch(k, ss);
-      if (e == cudaSuccess) e = cudaEventRecord(h->ev[2 * k + 1], ss);
-      return e;
-    });
-  }
-  return fan_out(h, st, launch);
+  // per-launch events in the profiling modes (serialised in mode 2), read by sf_get_slice_info
+  return run_call(h, true, D, h->d_D32.p, nullptr, nullptr, grad, cutoff, fp32_cutoff, st, h->profiling, nullptr);
 }
 
 int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *charges, int32_t natom, const double *D,

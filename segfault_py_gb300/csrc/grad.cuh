@@ -136,38 +136,57 @@ __device__ __forceinline__ void grad_t1(const KParams &kp, const QGeom<R> &g, co
   }
 }
 
-template <int LA, int LB, int LC, int LD, typename R, int T>
-__device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork &w, const R *__restrict__ D,
-                                             double *grad, bool shared_acc);
+template <int LA, int LB, int LC, int LD, typename R, int T, typename A>
+__device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork &w, const R *__restrict__ D, A *grad);
 
 // Gradient contributions of a CTA are summed in shared memory (3 slots per
 // atom) and written with one atomic per slot at the end: all quartets add
 // into the same 3*natom words, so per-quartet global atomics serialise.
 constexpr int kGradSmemAtoms = 512;   // larger molecules add to global memory directly
 
+// Per-CTA sums: FP32 for the FP32 kernels (shared-memory FP32 atomic adds are
+// native; FP64 ones are compare-and-swap loops whose FP64 adds, retried on
+// every collision of the lanes' atoms, kept the 1/64-rate FP64 pipe a third
+// to half busy), FP64 for the FP64 and double-float kernels.
+template <typename R>
+using GradAcc = typename std::conditional<std::is_same<R, float>::value, float, double>::type;
+
+__device__ __forceinline__ double acc_to_f64(float v) { return f2d_alu(v); }
+__device__ __forceinline__ double acc_to_f64(double v) { return v; }
+__device__ __forceinline__ float acc_value(float v, float) { return v; }
+template <typename V>
+__device__ __forceinline__ double acc_value(V v, double) { return to_f64(v); }
+
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __global__ void __launch_bounds__(kBlock) grad_kernel(KParams kp, ClassWork w, const R *__restrict__ D, double *grad) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using GP0 = GGrp<LA, LB, LC, LD, R, T>;
+  using A = GradAcc<R>;
   const bool cta_sum = kp.natom <= kGradSmemAtoms;
-  double *sgrad = reinterpret_cast<double *>(smem_raw + (T == 1 ? 0 : (size_t)(kBlock / T) * GP0::BUFN * sizeof(R)));
+  A *sgrad = reinterpret_cast<A *>(smem_raw + (T == 1 ? 0 : (size_t)(kBlock / T) * GP0::BUFN * sizeof(R)));
+  const int TP0 = T * w.psplit;
+  const int64_t nq = work_count(w);
+  const int64_t qfirst = ((int64_t)blockIdx.x * (kBlock / TP0)) / w.wsplit;
+  if (qfirst >= nq) return;   // the whole CTA is past the end of the list
   if (cta_sum) {
-    for (int i = threadIdx.x; i < 3 * kp.natom; i += blockDim.x) sgrad[i] = 0.0;
+    for (int i = threadIdx.x; i < 3 * kp.natom; i += blockDim.x) sgrad[i] = (A)0;
     __syncthreads();
   }
-  const int TP0 = T * w.psplit;
   const int64_t q0 = ((int64_t)blockIdx.x * (kBlock / TP0) + threadIdx.x / TP0) / w.wsplit;
-  if (q0 < w.n) grad_quartet<LA, LB, LC, LD, R, T>(kp, w, D, cta_sum ? sgrad : grad, cta_sum);
+  if (q0 < nq) {
+    if (cta_sum) grad_quartet<LA, LB, LC, LD, R, T, A>(kp, w, D, sgrad);
+    else grad_quartet<LA, LB, LC, LD, R, T, double>(kp, w, D, grad);
+  }
   if (cta_sum) {
     __syncthreads();
     for (int i = threadIdx.x; i < 3 * kp.natom; i += blockDim.x)
-      if (sgrad[i] != 0.0) atomicAdd(grad + i, sgrad[i]);
+      if (sgrad[i] != (A)0) atomicAdd(grad + i, acc_to_f64(sgrad[i]));
   }
 }
 
-template <int LA, int LB, int LC, int LD, typename R, int T>
+template <int LA, int LB, int LC, int LD, typename R, int T, typename A>
 __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork &w, const R *__restrict__ D,
-                                             double *grad, bool shared_acc) {
+                                             A *grad) {
   using Q = QC<LA, LB, LC, LD>;
   using G = QG<LA, LB, LC, LD>;
   using GP = GGrp<LA, LB, LC, LD, R, T>;
@@ -191,7 +210,6 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
   const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R *tab = reinterpret_cast<R *>(smem_raw) + (threadIdx.x / T) * GP::BUFN;
-  (void)shared_acc;
 
   // G_o of this lane's outputs (normalised, permutation count folded in),
   // packed table offsets and Cartesian exponents of a, b, c per direction
@@ -312,8 +330,8 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       gD[d] = -(gA[d] + gB[d] + gC[d]);
-      atomicAdd(grad + 3 * at_c + d, to_f64(gC[d]));
-      atomicAdd(grad + 3 * at_d + d, to_f64(gD[d]));
+      atomicAdd(grad + 3 * at_c + d, acc_value(gC[d], A()));
+      atomicAdd(grad + 3 * at_d + d, acc_value(gD[d], A()));
     }
     // centres a, b: with one quartet per lane, the lanes sharing the bra pair
     // (consecutive in the cost-sorted list) add their forces first
@@ -322,11 +340,31 @@ __device__ __forceinline__ void grad_quartet(const KParams &kp, const ClassWork 
     if (write) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        atomicAdd(grad + 3 * at_a + d, to_f64(gab[d]));
-        atomicAdd(grad + 3 * at_b + d, to_f64(gab[3 + d]));
+        atomicAdd(grad + 3 * at_a + d, acc_value(gab[d], A()));
+        atomicAdd(grad + 3 * at_b + d, acc_value(gab[3 + d], A()));
       }
     }
   }
+}
+
+// Primitive split of one gradient launch.  The energy kernel's split S = P*W
+// of the list is re-cut for this kernel's T (as many sub-groups inside the
+// T*P <= 32 lanes as fit, the rest as separate groups) and then doubled while
+// the list's lanes stay below 8 resident warps per SM sub-partition: a
+// derivative quartet costs several energy quartets, so the few-quartet
+// launches (the accurate tier above all) otherwise run at the latency of one
+// quartet's primitive loop on a fraction of the SMs.  Every sub-group keeps at
+// least one primitive quartet of the list's costliest quartet.
+inline ClassWork grad_work(const ClassWork &w, int T, int nsm) {
+  int S = (w.psplit < 1 ? 1 : w.psplit) * (w.wsplit < 1 ? 1 : w.wsplit);
+  const int64_t fill = (int64_t)(nsm < 1 ? 1 : nsm) * 4 * 8 * 32;
+  while (w.n * T * S < fill && 2 * S <= w.max_cost && 2 * S <= (32 / T) * kMaxWsplit) S *= 2;
+  int P = S;
+  while (T * P > 32) P >>= 1;
+  ClassWork w2 = w;
+  w2.psplit = P;
+  w2.wsplit = S / P < kMaxWsplit ? S / P : kMaxWsplit;
+  return w2;
 }
 
 template <int LA, int LB, int LC, int LD, typename R>

@@ -15,14 +15,8 @@ template <int LA, int LB, int LC, int LD>
 static cudaError_t run_grad_dd(const KParams &kp, const ClassWork &w, const dd *D, double *grad, cudaStream_t st) {
   constexpr int T = tgrad(QC<LA, LB, LC, LD>::NABCD);
   if (w.n <= 0) return cudaSuccess;
-  // the split S = P*W of the energy kernel's lanes, re-cut for this kernel's T
-  const int S = (w.psplit < 1 ? 1 : w.psplit) * (w.wsplit < 1 ? 1 : w.wsplit);
-  int P = S;
-  while (T * P > 32) P >>= 1;
-  ClassWork w2 = w;
-  w2.psplit = P;
-  w2.wsplit = std::min(S / P, kMaxWsplit);
-  const int G = kBlock / (T * P);
+  const ClassWork w2 = grad_work(w, T, kp.nsm);
+  const int G = kBlock / (T * w2.psplit);
   constexpr size_t smem = grad_smem<LA, LB, LC, LD, dd>();
   grad_kernel<LA, LB, LC, LD, dd, T><<<(unsigned)((w.n * w2.wsplit + G - 1) / G), kBlock, smem, st>>>(kp, w2, D, grad);
   return cudaGetLastError();

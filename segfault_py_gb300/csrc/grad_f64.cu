@@ -11,16 +11,8 @@ template <int LA, int LB, int LC, int LD>
 static cudaError_t run_grad64(const KParams &kp, const ClassWork &w, const double *D, double *grad, cudaStream_t st) {
   constexpr int T = tgrad(QC<LA, LB, LC, LD>::NABCD);
   if (w.n <= 0) return cudaSuccess;
-  // the split S = P*W chosen for the energy kernel's lanes, re-cut for this
-  // kernel's T: as many sub-groups inside the T*P <= 32 lanes as fit, the rest
-  // as separate groups
-  const int S = (w.psplit < 1 ? 1 : w.psplit) * (w.wsplit < 1 ? 1 : w.wsplit);
-  int P = S;
-  while (T * P > 32) P >>= 1;
-  ClassWork w2 = w;
-  w2.psplit = P;
-  w2.wsplit = std::min(S / P, kMaxWsplit);
-  const int G = kBlock / (T * P);
+  const ClassWork w2 = grad_work(w, T, kp.nsm);
+  const int G = kBlock / (T * w2.psplit);
   constexpr size_t smem = grad_smem<LA, LB, LC, LD, double>();
   grad_kernel<LA, LB, LC, LD, double, T><<<(unsigned)((w.n * w2.wsplit + G - 1) / G), kBlock, smem, st>>>(kp, w2, D, grad);
   return cudaGetLastError();

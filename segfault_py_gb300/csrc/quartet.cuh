@@ -1084,13 +1084,23 @@ __device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
 // ---------------------------------------------------------------------------
 struct ClassWork {
   const int2 *list;
-  int64_t n;
+  int64_t n;               // quartets in the list (with count: the list's capacity)
   int x0, y0;              // first global pair index of class X / Y
   int same;                // X == Y
   int psplit;              // P: primitive sub-groups per quartet inside one group of T*P <= 32 lanes
   int wsplit;              // W: groups per quartet; group c of W runs primitive sub-groups c*P .. c*P+P-1
                            // of W*P and digests its partial integrals itself (digestion is linear)
+  int max_cost = 1;        // K_ab K_cd of the list's first (costliest) quartet
+  // device count of the quartets actually in the list (lists compacted on the
+  // device by the density-weighted classification); nullptr: n
+  const unsigned long long *count = nullptr;
 };
+
+// quartets of a work list: the device count when the list was compacted on
+// the device, else the host count
+__device__ __forceinline__ int64_t work_count(const ClassWork &w) {
+  return w.count ? (int64_t)__ldg(w.count) : w.n;
+}
 
 constexpr int kBlock = 128;
 constexpr int kMaxWsplit = 64;
@@ -1113,9 +1123,10 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
     for (int k = threadIdx.x; k < NTAB4; k += blockDim.x) tab4[k] = __ldg(src + k);
     __syncthreads();
     const float *tab_s = reinterpret_cast<const float *>(smem_raw);
+    const int64_t nq = work_count(w);
     for (int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;; gid += (int64_t)gridDim.x * (kBlock / TP)) {
       const int64_t q = gid / W;
-      if (q >= w.n) return;
+      if (q >= nq) return;
       const int sub = (int)(gid - q * W) * P + p;
       const int2 ij = __ldg(w.list + q);
       const QGeom<R> g = make_geom32(kp, w.x0 + ij.x, w.y0 + ij.y);
@@ -1134,7 +1145,7 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
   const int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;
   const int64_t q = gid / W;
   const int sub = (int)(gid - q * W) * P + p;   // primitive sub-group of the W*P
-  if (q >= w.n) return;
+  if (q >= work_count(w)) return;
   const int2 ij = __ldg(w.list + q);
   const int i = ij.x, j = ij.y;
   const int pab = w.x0 + i, pcd = w.y0 + j;

@@ -110,6 +110,16 @@ class FockBuilder:
             _lib.check(_lib.lib().sf_schwarz(self._h, q.ctypes.data, _stream_ptr()))
         return q
 
+    def set_density_screening(self, on: bool = True, fock_fp32_cutoff: float = -1.0,
+                              grad_drop_cutoff: float = -1.0, grad_fp32_cutoff: float = -1.0):
+        """Density-weighted classification of every later Fock build and
+        gradient (sf_set_density_screening): the mixed modes run an
+        accurate-tier quartet in FP32 when its density-weighted bound is below
+        the FP32 cutoff; the gradient leaves out quartets whose bound is below
+        the drop cutoff.  Negative cutoffs: the call's own."""
+        _lib.check(_lib.lib().sf_set_density_screening(self._h, 1 if on else 0, fock_fp32_cutoff,
+                                                       grad_drop_cutoff, grad_fp32_cutoff))
+
     def set_partition(self, part: int, nparts: int):
         _lib.check(_lib.lib().sf_set_partition(self._h, part, nparts))
 

@@ -82,7 +82,8 @@ def main(argv=None):
     ap.add_argument("--slices", action="store_true")
     ap.add_argument("--timeline", action="store_true",
                     help="concurrent launches with start/end times (last build)")
-    ap.add_argument("--time", action="store_true", help="also time --builds normal (concurrent) builds with events")
+    ap.add_argument("--time", action="store_true",
+                    help="also time --builds normal (concurrent) builds (or gradients) with events")
     ap.add_argument("--autotune", action="store_true", help="autotune the launch shapes first")
     ap.add_argument("--grad", action="store_true",
                     help="profile the two-electron gradient (sf_grad_jk) instead of the Fock build")
@@ -143,6 +144,23 @@ def main(argv=None):
         print("\n".join(rows))
     if a.timeline and not a.slices:
         print("\n".join(timeline_table(fb)))
+    if a.time and a.grad:
+        from . import _lib
+        from .fock import _ptr, _stream_ptr
+        fb.set_profiling(0)
+        g = torch.zeros(3 * mol.natom, dtype=torch.float64, device=fb.device)
+        run = lambda: _lib.check(_lib.lib().sf_grad_jk(fb.handle, _ptr(D), _ptr(g), _lib.PRECISION[a.precision],
+                                                       a.cutoff, a.fp32_cutoff, _stream_ptr()))
+        for _ in range(3):
+            run()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(a.builds):
+            run()
+        ev[1].record()
+        torch.cuda.synchronize()
+        print("wall time of one two-electron gradient (mean of %d back to back): %.4f ms"
+              % (a.builds, ev[0].elapsed_time(ev[1]) / a.builds))
     if a.time and not a.grad:
         fb.set_profiling(0)
         J = torch.empty_like(D)

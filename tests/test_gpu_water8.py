@@ -1,0 +1,122 @@
+"""Parity at the configurations the numbers are quoted on.
+
+(H2O)8 6-31G* (152 AOs, seed 0), the Fock-build workload: J, K and energies of
+the library against the oracle's (tests/golden/water8_631gs.npz, written by
+tests/golden/make_water8.py from the reference's own molecule.py CGFs, the C
+restatement of core.f90's Rys engine with the reference's root5 fits, and the
+restated scf_diis of hf.py:237-353).  Tolerances: FP64 and double-float J/K
+1e-12 of max |J|, |K| and energies 1e-8 Eh; mixed modes energies 1e-6 Eh.
+
+(H2O)16 6-31G* (304 AOs, seed 0), the gradient workload: analytic FP64 and
+mixed (FP32 + double-float) gradients against central finite differences
+(step 1e-4 bohr) of FP64 GPU SCF energies on six coordinates, 1e-6 Eh/bohr.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = os.path.join(HERE, "golden", "water8_631gs.npz")
+CUTOFF = 1e-12
+FP32_CUTOFF = 1e-2
+STEP = 1e-4   # bohr
+
+
+def _sym(tril, n):
+    M = np.zeros((n, n))
+    M[np.tril_indices(n)] = tril
+    return M + np.tril(M, -1).T
+
+
+@pytest.fixture(scope="module")
+def w8():
+    z = np.load(FIXTURE)
+    n = int(z["nao"])
+    return dict(n=n, xyz=z["xyz_angstrom"], D=_sym(z["D"], n), J=_sym(z["J"], n), K=_sym(z["K"], n),
+                H=_sym(z["H"], n), e_total=float(z["e_total"]), e_elec=float(z["e_elec_at_D"]),
+                e_nuc=float(z["e_nuc"]))
+
+
+@pytest.fixture(scope="module")
+def w8_gpu(w8):
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.molecule import Molecule
+    sym, xyz = G.water_cluster(8, seed=0)
+    # the fixture's geometry (the generator's rotations agree across machines
+    # to rounding, not bit for bit); the integrals are taken at the stored one
+    assert np.abs(xyz - w8["xyz"]).max() < 1e-12
+    mol = Molecule.from_geometry(sym, w8["xyz"], "6-31g*")
+    assert mol.nao == w8["n"]
+    fb = FockBuilder(mol, device=torch.device("cuda:0"), cutoff=CUTOFF, fp32_cutoff=FP32_CUTOFF)
+    yield mol, fb
+    fb.close()
+
+
+def test_water8_nuclear_and_one_electron_vs_oracle(cuda, w8, w8_gpu):
+    mol, fb = w8_gpu
+    assert abs(mol.e_nuc - w8["e_nuc"]) < 1e-10
+    S, T, V = fb.one_electron()
+    H = (T + V).cpu().numpy()
+    assert np.abs(H - w8["H"]).max() < 1e-10
+
+
+@pytest.mark.parametrize("precision,jk_tol,e_tol", [("fp64", 1e-12, 1e-8), ("df", 1e-12, 1e-8),
+                                                    ("mixed", None, 1e-6), ("mixed_df", None, 1e-6)])
+def test_water8_jk_and_energy_vs_oracle(cuda, w8, w8_gpu, precision, jk_tol, e_tol):
+    mol, fb = w8_gpu
+    D = torch.tensor(w8["D"], device=cuda)
+    J, K = fb.jk(D, precision=precision)
+    J, K = J.cpu().numpy(), K.cpu().numpy()
+    if jk_tol is not None:
+        assert np.abs(J - w8["J"]).max() <= jk_tol * np.abs(w8["J"]).max()
+        assert np.abs(K - w8["K"]).max() <= jk_tol * np.abs(w8["K"]).max()
+    # E(D) = 1/2 sum D (2H + J - K/2) + E_nuc with the oracle's H: the error is the two-electron part's
+    e = 0.5 * float(np.sum(w8["D"] * (2.0 * w8["H"] + J - 0.5 * K))) + w8["e_nuc"]
+    assert abs(e - (w8["e_elec"] + w8["e_nuc"])) < e_tol, (precision, e - (w8["e_elec"] + w8["e_nuc"]))
+
+
+@pytest.mark.parametrize("precision,e_tol", [("fp64", 1e-8), ("mixed_df", 1e-6)])
+def test_water8_scf_energy_vs_oracle(cuda, w8, w8_gpu, precision, e_tol):
+    from segfault_py_gb300.scf import scf_diis
+    mol, fb = w8_gpu
+    r = scf_diis(mol, tol=1e-10, fb=fb, precision=precision)
+    assert r.converged
+    assert abs(r.energy - w8["e_total"]) < e_tol, (precision, r.energy - w8["e_total"])
+
+
+def test_water16_gradient_vs_fd_subset(cuda):
+    """Six coordinates spread over the cluster (O and H, x, y and z)."""
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.grad import rhf_gradient
+    from segfault_py_gb300.molecule import BOHR, Molecule
+    from segfault_py_gb300.scf import scf_diis
+    sym, xyz = G.water_cluster(16, seed=0)
+    x0 = xyz / BOHR
+    mol = Molecule.from_geometry(sym, xyz, "6-31g*")
+    fb = FockBuilder(mol, device=cuda, cutoff=CUTOFF, fp32_cutoff=FP32_CUTOFF)
+    r = scf_diis(mol, tol=1e-11, dtol=1e-8, fb=fb, precision="fp64")
+    g64 = rhf_gradient(mol, r, fb, precision="fp64").cpu().numpy()
+    gmx = rhf_gradient(mol, r, fb, precision="mixed_df").cpu().numpy()
+    fb.close()
+    assert np.abs(g64.sum(axis=0)).max() < 1e-8        # translational invariance
+
+    def energy(x_bohr):
+        m = Molecule.from_geometry(sym, x_bohr * BOHR, "6-31g*")
+        f = FockBuilder(m, device=cuda, cutoff=CUTOFF)
+        e = scf_diis(m, tol=1e-11, dtol=1e-8, maxiter=200, fb=f, precision="fp64").energy
+        f.close()
+        return e
+
+    for a, d in [(0, 0), (4, 1), (17, 2), (26, 0), (33, 1), (47, 2)]:
+        xp, xm = x0.copy(), x0.copy()
+        xp[a, d] += STEP
+        xm[a, d] -= STEP
+        fd = (energy(xp) - energy(xm)) / (2 * STEP)
+        assert abs(fd - g64[a, d]) < 1e-6, ("fp64", a, d, fd, g64[a, d])
+        assert abs(fd - gmx[a, d]) < 1e-6, ("mixed_df", a, d, fd, gmx[a, d])
