@@ -14,7 +14,9 @@ Reported:
                in HBM; L2 flushed
                (256 MB write) before every step, each step timed by CUDA events;
                each build launched eagerly through FockBuilder.jk
-               (graph_replay_value: the same build replayed from a CUDA graph)
+               (graph_replay_value: the same build replayed from a CUDA graph;
+               persistent_launch_value: the FP32 register-path classes as one
+               persistent launch per register tier, fed by a device work queue)
 * e2e          same metric through the public API with host buffers: pinned D
                -> device, Fock build, J and K -> pinned host, every step
 * fp64         the all-FP64 build, same protocol (the plain FP64 GPU baseline)
@@ -241,6 +243,7 @@ def run_ours(args):
         F = H + J - 0.5 * K
         return float(0.5 * torch.sum(D * (H + F)))
     e64, ehl, emx = energy("fp64"), energy(HEADLINE), energy("mixed")
+    vs_oracle = oracle_energy_errors(fb, mol, nwater, basis, dev)
 
     # stats + per-launch profile of one build per mode
     prof = {}
@@ -268,6 +271,12 @@ def run_ours(args):
     # the same build replayed from a captured CUDA graph, reported beside
     g_hl = fb.capture_jk(D, J, K, precision=HEADLINE)
     t_hl_graph = time_steps(g_hl.replay, args.steps, args.warmup, flush, stream)
+    # the same build with the FP32 register-path classes as persistent tier
+    # launches fed by a device work queue (sf_set_launch_mode), reported beside
+    fb.set_launch_mode("persistent")
+    t_hl_persist = time_steps(lambda: fb.jk(D, precision=HEADLINE, out=(J, K)), args.steps, args.warmup, flush,
+                              stream)
+    fb.set_launch_mode("streams")
     # e2e through the public API with host buffers
     Dh = D.cpu().pin_memory()
     Jh = torch.empty_like(Dh).pin_memory()
@@ -344,12 +353,14 @@ def run_ours(args):
                             "note": "FP32 below the cutoff, native FP64 above",
                             "energy_error_vs_fp64": emx - e64, "speedup_vs_fp64": ms_64 / ms_mx},
         "graph_replay_value": world * steps / (float(np.sum(t_hl_graph)) * 1e-3),
+        "persistent_launch_value": world * steps / (float(np.sum(t_hl_persist)) * 1e-3),
         "quartets_per_s": (st_hl["quartets_fp64"] + st_hl["quartets_fp32"]) * world * steps / (ms_hl * 1e-3),
         "prim_quartets_per_s": (st_hl["prim_quartets_fp64"] + st_hl["prim_quartets_fp32"]) * world * steps
                                / (ms_hl * 1e-3),
         "quartets": {"double_float": st_hl["quartets_fp64"], "fp32": st_hl["quartets_fp32"],
                      "unscreened": st_hl["quartets_total"]},
         "energy_error_mixed_vs_fp64": ehl - e64,
+        "energy_error_vs_oracle": vs_oracle,
         "forces": {"value": world * 1e3 / float(np.mean(t_f[HEADLINE])), "unit": "forces/s",
                    "fp64": world * 1e3 / float(np.mean(t_f["fp64"])),
                    "max_grad_error_mixed_vs_fp64": grad_err, "unit_error": "Eh/bohr",
@@ -377,6 +388,41 @@ def run_ours(args):
 
 
 # ----------------------------------------------------------------------------
+ORACLE_FIXTURE = os.path.join(REPO, "tests", "golden", "water8_631gs.npz")
+
+
+def oracle_energy_errors(fb, mol, nwater, basis, dev):
+    """Energy errors against the all-FP64 oracle at the oracle's converged
+    density, for the (H2O)8 6-31G* workload: the committed fixture holds the
+    oracle's D, H and E(D) = 1/2 sum D (2H + J - K/2) + E_nuc (the reference's
+    Rys algorithm with its root5 fits, every unique AO quartet).  Each build's
+    E(D) uses the fixture's H, so the error is the two-electron part's."""
+    import torch
+    if nwater != 8 or basis.lower() != "6-31g*" or not os.path.exists(ORACLE_FIXTURE):
+        return None
+    z = np.load(ORACLE_FIXTURE)
+    n = int(z["nao"])
+    from segfault_py_gb300 import geometry as G
+    _, xyz = G.water_cluster(8, seed=0)
+    if n != mol.nao or np.abs(xyz - z["xyz_angstrom"]).max() > 1e-10:
+        return None
+
+    def sym(t):
+        M = np.zeros((n, n))
+        M[np.tril_indices(n)] = t
+        return M + np.tril(M, -1).T
+    Dn, Hn = sym(z["D"]), sym(z["H"])
+    e_ref = float(z["e_elec_at_D"]) + float(z["e_nuc"])
+    Dt = torch.tensor(Dn, device=dev)
+    out = {"reference": "oracle fixture tests/golden/water8_631gs.npz (E(D) at the oracle's converged D, roots: %s)"
+                        % str(z["roots"])}
+    for prec in ("fp64", "mixed_df", "mixed"):
+        J, K = fb.jk(Dt, precision=prec)
+        J, K = J.cpu().numpy(), K.cpu().numpy()
+        out[prec] = 0.5 * float(np.sum(Dn * (2.0 * Hn + J - 0.5 * K))) + float(z["e_nuc"]) - e_ref
+    return out
+
+
 def setup_costs(mol, dev, D, J, K, reps=3):
     """Per-geometry cost, paid once per geometry (each step of an optimisation
     or MD loop), outside the Fock-build timing: a new handle (shell and pair

@@ -169,20 +169,49 @@ int sf_set_tuning(sf_handle *h, const sf_tune_entry *entries, int32_t n);
  * by every sf_fock_jk / sf_grad_jk call from its density D (no counterpart in
  * the reference, which computes every quartet in FP64).  With M_xy the
  * largest |D| element of the block of shells x, y:
- *  - Fock build, mixed modes: a quartet of the accurate tier (Q_ab Q_cd >=
- *    fp32_cutoff) stays there only while Q_ab Q_cd max(2M_ab, 2M_cd, M_ac,
- *    M_bd, M_ad, M_bc) -- a bound on what it adds to any element of J or K --
- *    is >= fock_fp32_cutoff; otherwise it runs in FP32;
- *  - gradient: a quartet whose Q_ab Q_cd (M_ab M_cd/2 + (M_ac M_bd +
- *    M_ad M_bc)/8) is below grad_drop_cutoff is left out; in the mixed modes
- *    one of the accurate tier with that bound below grad_fp32_cutoff runs in
- *    FP32.
- * A negative cutoff means the call's own: fp32_cutoff for the two FP32
- * cutoffs, the Schwarz cutoff for the drop cutoff.  on = 0 turns the
- * classification off (every call then uses the Schwarz-sorted lists as cut).
- * Default: on, all three cutoffs negative. */
-int sf_set_density_screening(sf_handle *h, int32_t on, double fock_fp32_cutoff, double grad_drop_cutoff,
+ *  - SF_DENS_FOCK, Fock build, mixed modes: a quartet of the accurate tier
+ *    (Q_ab Q_cd >= fp32_cutoff) stays there only while Q_ab Q_cd max(2M_ab,
+ *    2M_cd, M_ac, M_bd, M_ad, M_bc) -- a bound on what it adds to any element
+ *    of J or K -- is >= fock_fp32_cutoff; otherwise it runs in FP32.  Off by
+ *    default: the split then moves with D from one SCF iteration to the next,
+ *    which makes F(D) jump by the FP32 rounding of the quartets that change
+ *    tier and stalls the last decades of an SCF's convergence, for a gain of
+ *    about 1 % of the build time on water clusters;
+ *  - SF_DENS_GRAD, gradient: a quartet whose bound B = Q_ab Q_cd (M_ab
+ *    M_cd/2 + (M_ac M_bd + M_ad M_bc)/8) is below grad_drop_cutoff is left
+ *    out; in the mixed modes one of the accurate tier runs in FP32 when
+ *    B (s_a + s_b + s_c + s_d) is below grad_fp32_cutoff, s_x the square root
+ *    of shell x's largest exponent (a derivative integral outgrows the
+ *    Schwarz bound of its integral by about that factor).  On by default.
+ * A negative cutoff means the default: the call's fp32_cutoff for the Fock
+ * build's FP32 cutoff, 3e-2 times it for the gradient's (measured against
+ * FP64 with fp32_cutoff 1e-2: 6.9e-8 Eh/bohr on (H2O)16 in 6-31G*, 4.5e-7 on
+ * C20H42 in 6-31G**), the Schwarz cutoff for the drop cutoff.  flags = 0
+ * turns the classification off (every call then uses the Schwarz-sorted
+ * lists as cut).
+ * Default: SF_DENS_GRAD, all three cutoffs negative. */
+#define SF_DENS_FOCK 1
+#define SF_DENS_GRAD 2
+int sf_set_density_screening(sf_handle *h, int32_t flags, double fock_fp32_cutoff, double grad_drop_cutoff,
                              double grad_fp32_cutoff);
+
+/* How a Fock build launches its class kernels (no counterpart in the
+ * reference, whose scheduler is Pool(8).map over AO quartets, hf.py:45-47):
+ *  - SF_LAUNCH_STREAMS (default): one launch per (class, precision, primitive
+ *    split) slice, spread over 16 side streams forked from the caller's
+ *    stream and joined back;
+ *  - SF_LAUNCH_PERSISTENT: the FP32 register-path classes run as one
+ *    persistent launch per register tier (four tiers of similar register
+ *    use), each CTA taking CTA-sized tiles of the tier's lists from a device
+ *    work queue, heaviest first, until it is empty; the other lists keep their
+ *    own launches.  ctas_per_sm sets the persistent grid (0: the occupancy
+ *    limit of each tier kernel).  Profiling modes and gradients use the
+ *    stream launches.  The first build in this mode after the lists change
+ *    allocates the tile tables.
+ * The measured comparison is in the design notes; the default is the faster. */
+#define SF_LAUNCH_STREAMS 0
+#define SF_LAUNCH_PERSISTENT 1
+int sf_set_launch_mode(sf_handle *h, int32_t mode, int32_t ctas_per_sm);
 
 /* Restrict sf_fock_jk to the slice [part, part+1) of nparts equal-work slices
  * of every quartet class (replica / multi-GPU partitioning hook; 0,1 = all). */

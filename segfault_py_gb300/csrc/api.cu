@@ -176,9 +176,14 @@ __global__ void to_dd_kernel(const double *D, float2 *Dd, int64_t n) {
 //    >= its cutoff, else it runs in FP32 (demoted);
 //  * gradient: every contraction coefficient is bounded by
 //    G = M_ab M_cd / 2 + (M_ac M_bd + M_ad M_bc) / 8, so a quartet whose
-//    Q_ab Q_cd G is below the drop cutoff is left out (density screening) and
-//    one of the accurate tier with Q_ab Q_cd G below the accurate cutoff runs
-//    in FP32.
+//    Q_ab Q_cd G is below the drop cutoff is left out (density screening).
+//    A derivative integral is larger than the Schwarz bound of its integral
+//    by about the square root of the differentiated exponent (d/dA_x of a
+//    primitive is 2 alpha x_A times it, whose norm grows as sqrt(alpha)), so
+//    one of the accurate tier runs in FP32 when
+//    Q_ab Q_cd G (s_a + s_b + s_c + s_d), s = sqrt of the shell's largest
+//    exponent, is below the accurate cutoff: quartets of tight core shells
+//    stay accurate.
 // Every list is compacted into a "kept" and a "demoted" list at the same
 // offsets (d_keep, d_dem), order kept within each chunk of 1024 entries, with
 // device counts read by the kernels, so nothing synchronises with the host.
@@ -189,6 +194,11 @@ struct ClassifySlice {
   int pad;
 };
 constexpr int kClsThreads = 256, kClsPer = 4, kClsChunk = kClsThreads * kClsPer;
+// default gradient FP32 cutoff / the call's fp32_cutoff, measured against
+// FP64 gradients (6-31G* (H2O)16 / 6-31G** C20H42, FP32 cutoff 1e-2): 3e-4
+// gives 6.9e-8 / 4.5e-7 Eh/bohr, 1e-3 1.4e-7 / 1.05e-6, 1e-2 1.4e-6 / 9.8e-6
+// (the FP32 tier alone leaves 7e-8 / 3e-7)
+constexpr double kGradFp32Scale = 3e-2;
 
 // M_xy = max |D| over the Cartesian block of shells x, y (FP32 is enough for a bound)
 __global__ void shell_dmax_kernel(const double *D, int n, const int *l, const int *ao, int ns, float *dm) {
@@ -205,8 +215,8 @@ __global__ void shell_dmax_kernel(const double *D, int n, const int *l, const in
 
 __global__ void __launch_bounds__(kClsThreads) classify_kernel(
     const int2 *list, const ClassifySlice *sl, const int2 *blk, const int *pa, const int *pb, const int *pnp,
-    const double *pq, const float *dm, int ns, int grad_mode, double t_drop, double t_acc, int2 *keep, int2 *dem,
-    unsigned long long *cnt) {
+    const double *pq, const float *dm, const float *sqa, int ns, int grad_mode, double t_drop, double t_acc,
+    int2 *keep, int2 *dem, unsigned long long *cnt) {
   const int2 bk = blk[blockIdx.x];
   const ClassifySlice S = sl[bk.x];
   const int64_t e0 = (int64_t)bk.y * kClsChunk + (int64_t)threadIdx.x * kClsPer;
@@ -225,10 +235,15 @@ __global__ void __launch_bounds__(kClsThreads) classify_kernel(
     const float mab = dm[a * ns + b], mcd = dm[c * ns + d], mac = dm[a * ns + c], mbd = dm[b * ns + d],
                 mad = dm[a * ns + d], mbc = dm[b * ns + c];
     const double q = pq[pab] * pq[pcd];
-    double bound;
-    if (grad_mode) bound = q * (double)(0.5f * mab * mcd + 0.125f * (mac * mbd + mad * mbc));
-    else bound = q * (double)fmaxf(2.0f * fmaxf(mab, mcd), fmaxf(fmaxf(mac, mbd), fmaxf(mad, mbc)));
-    where[k] = bound < t_drop ? 2 : (S.acc && bound < t_acc) ? 1 : 0;
+    double bound, bound_acc;
+    if (grad_mode) {
+      bound = q * (double)(0.5f * mab * mcd + 0.125f * (mac * mbd + mad * mbc));
+      bound_acc = bound * (double)(sqa[a] + sqa[b] + sqa[c] + sqa[d]);
+    } else {
+      bound = q * (double)fmaxf(2.0f * fmaxf(mab, mcd), fmaxf(fmaxf(mac, mbd), fmaxf(mad, mbc)));
+      bound_acc = bound;
+    }
+    where[k] = bound < t_drop ? 2 : (S.acc && bound_acc < t_acc) ? 1 : 0;
     const unsigned long long c0 = (unsigned long long)pnp[pab] * (unsigned long long)pnp[pcd];
     if (where[k] == 0) { ++nk; pk += c0; }
     if (where[k] == 1) { ++nd; pd += c0; }
@@ -346,9 +361,10 @@ struct sf_handle {
   // density-weighted classification (see classify_kernel); cutoffs < 0 mean
   // the call's own: fp32_cutoff for the accurate tiers, the Schwarz cutoff
   // for the gradient's drop bound
-  int dens_on = 1;
+  int dens_flags = SF_DENS_GRAD;   // SF_DENS_FOCK | SF_DENS_GRAD
   double dens_fock_acc = -1.0, dens_grad_drop = -1.0, dens_grad_acc = -1.0;
   DBuf<float> d_dmax;                      // nshell^2 block maxima of |D|
+  DBuf<float> d_sqa;                       // per shell: sqrt of its largest primitive exponent
   DBuf<int2> d_keep, d_dem;                // compacted lists at the offsets of d_list
   DBuf<unsigned long long> d_cnt;          // per slice: kept, demoted quartets; kept, demoted primitive quartets
   DBuf<ClassifySlice> d_csl;
@@ -359,9 +375,25 @@ struct sf_handle {
   struct Launch {
     int slice, kind, stream, demoted;
     ClassWork w;
+    int covered = 0;                       // run by a persistent tier launch, not by its own
   };
   std::vector<Launch> plan;
   bool plan_counts = false;                // quartet counts of the plan live on the device
+  // launch mode SF_LAUNCH_PERSISTENT: the FP32 register-path lists of a Fock
+  // build run as one persistent launch per register tier (jk_persist.cu)
+  int launch_mode = SF_LAUNCH_STREAMS;
+  int persist_ctas_per_sm = 0;             // 0: the occupancy limit of each tier kernel
+  int lists_version = 0, persist_version = -1;
+  DBuf<ClassWork> d_pworks;                // the covered lists
+  DBuf<int> d_pcls;
+  DBuf<int2> d_ptiles;                     // per tier, heaviest first
+  DBuf<unsigned> d_pnext;                  // one queue counter per tier
+  int ptile_off[kPersistTiers + 1] = {0};
+  std::vector<char> slice_covered;
+  struct TierLaunch {
+    int tier, stream, grid;
+  };
+  std::vector<TierLaunch> pplan;
 };
 
 namespace {
@@ -689,6 +721,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     SF_CK(h->d_cnt.alloc(4 * std::max<size_t>(h->slices.size(), 1)));
     SF_CK(h->d_dmax.alloc((size_t)h->nshell * h->nshell));
   }
+  ++h->lists_version;
   h->c_prec = prec;
   h->c_cut = cut;
   h->c_cut32 = cut32;
@@ -705,15 +738,16 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
 int density_classify(sf_handle *h, const double *D, bool grad, double cut, double cut32, cudaStream_t st,
                      int *launches, int *active) {
   *active = 0;
-  if (!h->dens_on || h->slices.empty()) return SF_OK;
+  if (!(h->dens_flags & (grad ? SF_DENS_GRAD : SF_DENS_FOCK)) || h->slices.empty()) return SF_OK;
   bool has32 = false, hasacc = false;
   for (const auto &sl : h->slices) (sl.prec == 1 ? has32 : hasacc) = true;
   const bool mixed = has32 && hasacc;
   if (!grad && !mixed) return SF_OK;
-  const double t_acc = mixed ? ((grad ? h->dens_grad_acc : h->dens_fock_acc) >= 0.0
-                                    ? (grad ? h->dens_grad_acc : h->dens_fock_acc)
-                                    : cut32)
-                             : -1.0;
+  // default FP32 cutoffs: the call's own for the Fock build, kGradFp32Scale
+  // times it for the gradient
+  const double t_acc = !mixed ? -1.0
+                       : grad ? (h->dens_grad_acc >= 0.0 ? h->dens_grad_acc : cut32 * kGradFp32Scale)
+                              : (h->dens_fock_acc >= 0.0 ? h->dens_fock_acc : cut32);
   const double t_drop = grad ? (h->dens_grad_drop >= 0.0 ? h->dens_grad_drop : cut) : -1.0;
   const int nb = grad ? h->nblk_all : h->nblk_acc;
   const int ns = h->nshell;
@@ -724,7 +758,7 @@ int density_classify(sf_handle *h, const double *D, bool grad, double cut, doubl
   if (nb > 0) {
     classify_kernel<<<(unsigned)nb, kClsThreads, 0, st>>>(
         h->d_list.p, h->d_csl.p, grad ? h->d_blk_all.p : h->d_blk_acc.p, h->d_pa.p, h->d_pb.p, h->d_pnp.p, h->d_pq.p,
-        h->d_dmax.p, ns, grad ? 1 : 0, t_drop, t_acc, h->d_keep.p, h->d_dem.p, h->d_cnt.p);
+        h->d_dmax.p, h->d_sqa.p, ns, grad ? 1 : 0, t_drop, t_acc, h->d_keep.p, h->d_dem.p, h->d_cnt.p);
     SF_CK(cudaGetLastError());
   }
   if (launches) *launches += nb > 0 ? 2 : 1;
@@ -732,12 +766,73 @@ int density_classify(sf_handle *h, const double *D, bool grad, double cut, doubl
   return SF_OK;
 }
 
+// Tile tables of the persistent tier launches for the current lists: every
+// FP32 slice of a class in a register tier is cut into tiles of kBlock / P
+// quartet groups (one CTA trip of the class kernel); a tier's tiles are
+// ordered by estimated cost, heaviest first (primitive quartets x roots x
+// (outputs + 30) per tile, from the slice's mean cost), so the long tiles
+// start first and the short ones fill the end.
+int build_persist(sf_handle *h) {
+  std::vector<ClassWork> works;
+  std::vector<int> cls;
+  struct T {
+    double cost;
+    int tier, work, tile;
+  };
+  std::vector<T> tiles;
+  h->slice_covered.assign(h->slices.size(), 0);
+  for (size_t k = 0; k < h->slices.size(); ++k) {
+    const auto &sl = h->slices[k];
+    const int tier = sl.prec == 1 ? persist_tier_of(sl.cls) : -1;
+    if (tier < 0 || sl.w.n <= 0) continue;
+    h->slice_covered[k] = 1;
+    const int P = std::max(1, sl.w.psplit), W = std::max(1, sl.w.wsplit);
+    const int64_t groups = sl.w.n * W, per = kBlock / P;
+    const int64_t nt = (groups + per - 1) / per;
+    const ClassInfo &ci = kClassInfo[sl.cls];
+    const double nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
+    const double nc = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
+    const double per_q = (double)sl.prims / (double)std::max<int64_t>(sl.quartets, 1) * nr * (nc + 30.0);
+    const int widx = (int)works.size();
+    works.push_back(sl.w);
+    cls.push_back(sl.cls);
+    for (int64_t c = 0; c < nt; ++c) {
+      const int64_t g0 = c * per, g1 = std::min(groups, g0 + per);
+      tiles.push_back(T{per_q * (double)(g1 - g0) / W, tier, widx, (int)c});
+    }
+  }
+  std::stable_sort(tiles.begin(), tiles.end(), [](const T &a, const T &b) {
+    return a.tier != b.tier ? a.tier < b.tier : a.cost > b.cost;
+  });
+  std::vector<int2> tl(tiles.size());
+  for (int t = 0; t <= kPersistTiers; ++t) h->ptile_off[t] = 0;
+  for (size_t i = 0; i < tiles.size(); ++i) {
+    tl[i] = make_int2(tiles[i].work, tiles[i].tile);
+    ++h->ptile_off[tiles[i].tier + 1];
+  }
+  for (int t = 0; t < kPersistTiers; ++t) h->ptile_off[t + 1] += h->ptile_off[t];
+  SF_CK(h->d_pworks.upload(works));
+  SF_CK(h->d_pcls.upload(cls));
+  SF_CK(h->d_ptiles.upload(tl));
+  SF_CK(h->d_pnext.alloc(kPersistTiers));
+  h->persist_version = h->lists_version;
+  return SF_OK;
+}
+
 // The launches of one call: one per slice (reading its compacted list when
 // the classification ran for it) and, for a classified accurate-tier slice of
 // a mixed mode, one FP32 launch of its demoted quartets on the next FP32
-// stream.
-void make_plan(sf_handle *h, bool grad, int active) {
+// stream.  In the persistent launch mode (Fock builds, profiling off) the
+// slices of the register tiers are marked covered and one launch per tier
+// runs them, on the FP32 streams.
+int make_plan(sf_handle *h, bool grad, int active) {
   h->plan.clear();
+  h->pplan.clear();
+  const bool persist = h->launch_mode == SF_LAUNCH_PERSISTENT && !grad && h->profiling == 0;
+  if (persist && h->persist_version != h->lists_version) {
+    const int rc = build_persist(h);
+    if (rc) return rc;
+  }
   h->plan_counts = active != 0;
   bool has32 = false, hasacc = false;
   for (const auto &sl : h->slices) (sl.prec == 1 ? has32 : hasacc) = true;
@@ -765,6 +860,18 @@ void make_plan(sf_handle *h, bool grad, int active) {
       h->plan.push_back(Dm);
     }
   }
+  if (persist) {
+    for (auto &L : h->plan)
+      if (!L.demoted && L.kind == 1 && h->slice_covered[L.slice]) L.covered = 1;
+    for (int t = 0; t < kPersistTiers; ++t) {
+      if (h->ptile_off[t + 1] == h->ptile_off[t]) continue;
+      int bps = h->persist_ctas_per_sm;
+      if (bps <= 0) SF_CK(persist_blocks_per_sm(t, &bps));
+      const int grid = std::max(1, h->nsm) * std::max(1, bps);
+      h->pplan.push_back(sf_handle::TierLaunch{t, sf_handle::kHiStreams + t, grid});
+    }
+  }
+  return SF_OK;
 }
 
 // Run fn(k, stream) for every slice k on its side stream (forked from st,
@@ -829,15 +936,25 @@ int run_plan(sf_handle *h, bool grad, const double *D, const float *D32, double 
   }
   SF_CK(cudaEventRecord(h->fork_ev, st));
   bool used[sf_handle::kSideStreams] = {false};
-  for (const auto &L : h->plan) used[L.stream] = true;
+  for (const auto &L : h->plan)
+    if (!L.covered) used[L.stream] = true;
+  for (const auto &T : h->pplan) used[T.stream] = true;
   for (int j = 0; j < sf_handle::kSideStreams; ++j)
     if (used[j]) SF_CK(cudaStreamWaitEvent(h->side[j], h->fork_ev, 0));
   for (size_t k = 0; k < h->plan.size(); ++k) {
     const auto &L = h->plan[k];
+    if (L.covered) continue;
     cudaStream_t ss = h->side[L.stream];
     if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k], ss));
     SF_CK(launch_one(h, L, grad, D, D32, Jh, Kh, g, ss));
     if (profiling) SF_CK(cudaEventRecord(h->ev[2 * k + 1], ss));
+    if (launches) ++*launches;
+  }
+  // the persistent tier launches last: they take the SM slots the others leave
+  for (const auto &T : h->pplan) {
+    PersistWork pw{h->d_pworks.p, h->d_pcls.p, h->d_ptiles.p + h->ptile_off[T.tier],
+                   h->ptile_off[T.tier + 1] - h->ptile_off[T.tier], h->d_pnext.p + T.tier};
+    SF_CK(launch_jk_persist_f32(T.tier, h->kp, pw, T.grid, D32, Jh, Kh, h->side[T.stream]));
     if (launches) ++*launches;
   }
   for (int j = 0; j < sf_handle::kSideStreams; ++j)
@@ -854,7 +971,8 @@ int run_call(sf_handle *h, bool grad, const double *D, const float *D32, double 
   int active = 0;
   int rc = density_classify(h, D, grad, cut, cut32, st, launches, &active);
   if (rc) return rc;
-  make_plan(h, grad, active);
+  rc = make_plan(h, grad, active);
+  if (rc) return rc;
   if (profiling) {
     rc = profiling_events(h, st);
     if (rc) return rc;
@@ -1225,6 +1343,15 @@ int sf_create(const sf_shell_desc *shells, int32_t nshell, sf_handle **out) {
   SF_CK(h->d_cy.upload(h->cy));
   SF_CK(h->d_cz.upload(h->cz));
   SF_CK(h->d_exps.upload(h->exps));
+  {
+    std::vector<float> sqa(h->nshell);
+    for (int a = 0; a < h->nshell; ++a) {
+      double m = 0.0;
+      for (int i = h->spoff[a]; i < h->spoff[a + 1]; ++i) m = std::max(m, h->exps[i]);
+      sqa[a] = (float)std::sqrt(m);
+    }
+    SF_CK(h->d_sqa.upload(sqa));
+  }
   SF_CK(h->d_coefs.upload(h->coefs));
   const HostTables &T = host_tables();
   SF_CK(h->d_tab64.upload(T.t64));
@@ -1389,15 +1516,25 @@ int sf_schwarz(sf_handle *h, double *q_out, void *stream) {
   return SF_OK;
 }
 
-int sf_set_density_screening(sf_handle *h, int32_t on, double fock_fp32_cutoff, double grad_drop_cutoff,
+int sf_set_density_screening(sf_handle *h, int32_t flags, double fock_fp32_cutoff, double grad_drop_cutoff,
                              double grad_fp32_cutoff) {
   if (!h) return fail(SF_EINVAL, "sf_set_density_screening: NULL handle");
+  if (flags & ~(SF_DENS_FOCK | SF_DENS_GRAD)) return fail(SF_EINVAL, "sf_set_density_screening: unknown flag");
   if (std::isnan(fock_fp32_cutoff) || std::isnan(grad_drop_cutoff) || std::isnan(grad_fp32_cutoff))
     return fail(SF_EINVAL, "sf_set_density_screening: NaN cutoff");
-  h->dens_on = on ? 1 : 0;
+  h->dens_flags = flags;
   h->dens_fock_acc = fock_fp32_cutoff;
   h->dens_grad_drop = grad_drop_cutoff;
   h->dens_grad_acc = grad_fp32_cutoff;
+  return SF_OK;
+}
+
+int sf_set_launch_mode(sf_handle *h, int32_t mode, int32_t ctas_per_sm) {
+  if (!h) return fail(SF_EINVAL, "sf_set_launch_mode: NULL handle");
+  if (mode != SF_LAUNCH_STREAMS && mode != SF_LAUNCH_PERSISTENT) return fail(SF_EINVAL, "sf_set_launch_mode: bad mode");
+  if (ctas_per_sm < 0 || ctas_per_sm > 64) return fail(SF_EINVAL, "sf_set_launch_mode: bad CTAs per SM");
+  h->launch_mode = mode;
+  h->persist_ctas_per_sm = ctas_per_sm;
   return SF_OK;
 }
 
@@ -1674,6 +1811,10 @@ int sf_fock_jk_noalloc(sf_handle *h, const double *D, double *J, double *K, int3
                 "sf_fock_jk_noalloc: the quartet lists for this precision and these cutoffs are not built; "
                 "call sf_fock_jk once with the same arguments first (that call allocates)");
   if (h->device < 0 || h->device >= 128) return fail(SF_EINVAL, "sf_fock_jk_noalloc: device index out of range");
+  if (h->launch_mode == SF_LAUNCH_PERSISTENT && h->profiling == 0 && h->persist_version != h->lists_version)
+    return fail(SF_ESTATE,
+                "sf_fock_jk_noalloc: the persistent launch tables are not built; call sf_fock_jk once in this launch "
+                "mode first (that call allocates)");
   DeviceGuard g(h->device);
   double *scratch = nullptr;
   {

@@ -10,6 +10,22 @@ cudaError_t launch_jk_f32(int cls, const KParams &kp, const ClassWork &w, const 
                           cudaStream_t st);
 cudaError_t launch_jk_dd(int cls, const KParams &kp, const ClassWork &w, const dd *D, double *Jh, double *Kh,
                          cudaStream_t st);
+// persistent multi-class FP32 J/K kernels (jk_persist.cu): one launch per
+// register tier runs the tiles of every list of the tier's classes, taken
+// from a device work queue
+constexpr int kPersistTiers = 4;
+struct PersistWork {
+  const ClassWork *works;   // the tier's lists
+  const int *cls;           // class of each list
+  const int2 *tiles;        // (list, tile index in the list), heaviest first
+  int ntiles;
+  unsigned *next;           // queue counter (zeroed by the launcher)
+};
+// tier of a class whose FP32 kernel runs in the register path, else -1
+int persist_tier_of(int cls);
+cudaError_t persist_blocks_per_sm(int tier, int *blocks);
+cudaError_t launch_jk_persist_f32(int tier, const KParams &kp, const PersistWork &pw, int grid, const float *D,
+                                  double *Jh, double *Kh, cudaStream_t st);
 // raw integrals of one class (fp32: FP32 evaluation, else FP64)
 cudaError_t launch_eri(int cls, int fp32, const KParams &kp, const EriWork &w, cudaStream_t st);
 cudaError_t launch_eri_dd(int cls, const KParams &kp, const EriWork &w, cudaStream_t st);

@@ -206,9 +206,11 @@ cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st) {
 //  * V: the bra and ket derivative share R_tuv(p, P - C) of each nucleus C,
 //    which receives minus their sum (translational invariance of
 //    <a|1/r_C|b>).
-// CTA per canonical pair (a, b), 64 threads.  For every primitive pair:
+// CTA per canonical pair (a, b), 64 threads.  For every primitive pair whose
+// bound (product Gaussian x block max of |D|, |W| x derivative, kinetic and
+// attraction factors) is not below 1e-15:
 //  * E coefficients (bra to LA+1, ket to LB+2) into shared memory;
-//  * the S and T bra-derivative terms by thread 0;
+//  * the S and T bra-derivative terms, one (i, j, direction) per thread;
 //  * the density-contracted Hermite coefficients of the bra and the ket
 //    derivative, M^d_tuv = 2pi/p c_i c_j sum_{i in a, j in b} D_ij sum_+- f
 //    E.. E.. E.. (nucleus independent), cooperatively into shared memory;
@@ -218,30 +220,82 @@ cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st) {
 //    dV/dX_d = -Z_C sum_tuv M^d_tuv R_tuv.
 constexpr int kOneGradThreads = 64;
 
+// shared-memory doubles of one_pair_grad2<LA, LB>: E coefficients, the bra and
+// ket Hermite coefficients MA, MB, the density block and the reduction rows
 template <int LA, int LB>
-__device__ void one_pair_grad2(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b) {
+constexpr int one_grad_smem() {
+  return 3 * (LA + 2) * (LB + 3) * (LA + LB + 4) + 6 * (LA + LB + 2) * (LA + LB + 2) * (LA + LB + 2) +
+         ncart(LA) * ncart(LB) + 6 * kOneGradThreads;
+}
+constexpr int kOneGradSmem = one_grad_smem<2, 2>();   // the largest
+
+template <int LA, int LB>
+__device__ void one_pair_grad2(const OneParams &P, const double *Dm, const double *Wm, double *grad, int a, int b,
+                               double *smem) {
   constexpr int NA = ncart(LA), NB = ncart(LB);
   constexpr int LE = LA + 1, L = LA + LB + 1, NH = (L + 1) * (L + 1) * (L + 1);
   constexpr int NRT = L / 2 + 1;   // Rys points whose rule is exact for F_0 .. F_L
+  constexpr int EN = (LE + 1) * (LB + 3) * (LE + LB + 3);
   const double pi = 3.14159265358979323846;
-  __shared__ double E[3][LE + 1][LB + 3][LE + LB + 3];
-  __shared__ double MA[3][NH], MB[3][NH];
-  __shared__ double Dab[NA][NB];
-  __shared__ double red[kOneGradThreads][6];
+  // carved from the kernel's one shared buffer (each instantiation declaring
+  // its own arrays made the kernel hold all nine sets, 79.5 KB)
+  using EArr = double[LE + 1][LB + 3][LE + LB + 3];
+  EArr *E = reinterpret_cast<EArr *>(smem);
+  double(*MA)[NH] = reinterpret_cast<double(*)[NH]>(smem + 3 * EN);
+  double(*MB)[NH] = MA + 3;
+  double(*Dab)[NB] = reinterpret_cast<double(*)[NB]>(smem + 3 * EN + 6 * NH);
+  double(*red)[6] = reinterpret_cast<double(*)[6]>(smem + 3 * EN + 6 * NH + NA * NB);
+  static_assert(3 * EN + 6 * NH + NA * NB + 6 * kOneGradThreads == one_grad_smem<LA, LB>(), "smem layout");
   const int tid = threadIdx.x;
   const bool two = a != b;   // canonical pair with a distinct ket: ket derivative too
   const double A[3] = {P.sh.cx[a], P.sh.cy[a], P.sh.cz[a]};
   const double B[3] = {P.sh.cx[b], P.sh.cy[b], P.sh.cz[b]};
   const int a0 = P.sh.ao[a], b0 = P.sh.ao[b], n = P.nao;
+  // block maximum of |D| and |W| and the summed nuclear charge: the scale of
+  // everything this pair adds, for the primitive-pair screening below
+  double dw = 0.0, zs = 0.0;
   for (int k = tid; k < NA * NB; k += blockDim.x) {
     const int i = k / NB, j = k % NB;
-    Dab[i][j] = Dm[(a0 + i) * n + b0 + j] * cart_norm(LA, i) * cart_norm(LB, j);
+    const double nrm = cart_norm(LA, i) * cart_norm(LB, j);
+    Dab[i][j] = Dm[(a0 + i) * n + b0 + j] * nrm;
+    dw = fmax(dw, fmax(fabs(Dab[i][j]), fabs(Wm[(a0 + i) * n + b0 + j] * nrm)));
   }
+  for (int k = tid; k < P.natom; k += blockDim.x) zs += fabs(P.charges[k]);
+  for (int off = 16; off > 0; off >>= 1) {
+    dw = fmax(dw, __shfl_xor_sync(0xffffffffu, dw, off));
+    zs += __shfl_xor_sync(0xffffffffu, zs, off);
+  }
+  if ((tid & 31) == 0) {
+    red[tid >> 5][0] = dw;
+    red[tid >> 5][1] = zs;
+  }
+  __syncthreads();
+  dw = 0.0;
+  zs = 0.0;
+  for (int w = 0; w < (int)blockDim.x / 32; ++w) {
+    dw = fmax(dw, red[w][0]);
+    zs += red[w][1];
+  }
+  __syncthreads();   // red is written again by the final reduction
+  double R2 = 0.0;
+  for (int d = 0; d < 3; ++d) R2 += (A[d] - B[d]) * (A[d] - B[d]);
   double gST[3] = {0.0, 0.0, 0.0}, gVA[3] = {0.0, 0.0, 0.0}, gVB[3] = {0.0, 0.0, 0.0};
   for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
     for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
       const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
       const double cc = P.coefs[ia] * P.coefs[ib];
+      // primitive pairs whose contributions all stay below 1e-15 are skipped
+      // (the same on every thread, so the barriers below stay uniform): the
+      // product Gaussian c_i c_j exp(-mu |AB|^2) (pi/p)^3/2 bounds the
+      // overlap; E coefficients grow at most as (|AB| + 1/sqrt(p) + 1)^(L+1),
+      // derivatives as 2 max(alpha, beta) + L, kinetic terms as
+      // 3 beta (LB + 2), attraction as 2 sqrt(p/pi) times the summed charge
+      {
+        const double g = fabs(cc) * exp(-mu * R2) * pow(pi / p, 1.5) * dw;
+        const double e = pow(sqrt(R2) + rsqrt(p) + 1.0, (double)(L + 1));
+        const double f = (2.0 * fmax(al, be) + L) * (1.0 + 2.0 * sqrt(p / pi) * zs + 3.0 * fmax(al, be) * (LB + 2));
+        if (g * e * f < 1e-15) continue;
+      }
       double Pc[3];
       for (int d = 0; d < 3; ++d) Pc[d] = (al * A[d] + be * B[d]) / p;
       __syncthreads();   // previous iteration done with E, M
@@ -255,15 +309,16 @@ __device__ void one_pair_grad2(const OneParams &P, const double *Dm, const doubl
             for (int t = 0; t <= LE + LB + 2; ++t) E[d][i][j][t] = Et[i][j][t];
       }
       __syncthreads();
-      // overlap / kinetic bra derivatives (Pulay -W dS, D dT)
-      if (tid == 0) {
+      // overlap / kinetic bra derivatives (Pulay -W dS, D dT), one (i, j, d)
+      // per thread (gST is summed over the CTA at the end)
+      {
         const double sp = pow(pi / p, 1.5);
-        for (int i = 0; i < NA; ++i)
-          for (int j = 0; j < NB; ++j) {
+        for (int task = tid; task < NA * NB * 3; task += blockDim.x) {
+            const int i = task / (NB * 3), j = (task / 3) % NB, d = task % 3;
             const double nrm = cart_norm(LA, i) * cart_norm(LB, j);
             const double Dij = Dab[i][j], Wij = Wm[(a0 + i) * n + b0 + j] * nrm;
             const int bx[3] = {cart_e(LB, j, 0), cart_e(LB, j, 1), cart_e(LB, j, 2)};
-            for (int d = 0; d < 3; ++d) {
+            {
               double dS = 0.0, dT = 0.0;
               for (int sgn = 0; sgn < 2; ++sgn) {
                 int ax[3] = {cart_e(LA, i, 0), cart_e(LA, i, 1), cart_e(LA, i, 2)};
@@ -352,29 +407,41 @@ __device__ void one_pair_grad2(const OneParams &P, const double *Dm, const doubl
             F[m] = f;
           }
         }
-        double R[L + 1][L + 1][L + 1][L + 1];
-        for (int m = 0; m <= L; ++m) {
-          double f = F[m];
-          for (int k = 0; k < m; ++k) f *= -2.0 * p;
-          R[m][0][0][0] = f;
-        }
-        for (int m = L - 1; m >= 0; --m)
-          for (int t = 0; t <= L - m; ++t)
-            for (int u = 0; u <= L - m - t; ++u)
-              for (int w = 0; w <= L - m - t - u; ++w) {
-                if (t + u + w == 0) continue;
+        // R^m_tuv by the Hermite Coulomb recursion, in place: level m
+        // overwrites t+u+w = L-m .. 1 from the top down (each entry needs
+        // level m+1 at t+u+w-1 and -2, not yet overwritten), then R^m_000
+        double R[L + 1][L + 1][L + 1];
+        double fm2p[L + 1];
+        fm2p[0] = 1.0;
+#pragma unroll
+        for (int m = 1; m <= L; ++m) fm2p[m] = fm2p[m - 1] * (-2.0 * p);
+        R[0][0][0] = F[L] * fm2p[L];
+#pragma unroll
+        for (int m = L - 1; m >= 0; --m) {
+#pragma unroll
+          for (int sl = L - m; sl >= 1; --sl)
+#pragma unroll
+            for (int t = 0; t <= sl; ++t)
+#pragma unroll
+              for (int u = 0; u <= sl - t; ++u) {
+                const int w = sl - t - u;
                 double r;
-                if (t > 0) r = (t > 1 ? (t - 1) * R[m + 1][t - 2][u][w] : 0.0) + pc[0] * R[m + 1][t - 1][u][w];
-                else if (u > 0) r = (u > 1 ? (u - 1) * R[m + 1][t][u - 2][w] : 0.0) + pc[1] * R[m + 1][t][u - 1][w];
-                else r = (w > 1 ? (w - 1) * R[m + 1][t][u][w - 2] : 0.0) + pc[2] * R[m + 1][t][u][w - 1];
-                R[m][t][u][w] = r;
+                if (t > 0) r = (t > 1 ? (t - 1) * R[t - 2][u][w] : 0.0) + pc[0] * R[t - 1][u][w];
+                else if (u > 0) r = (u > 1 ? (u - 1) * R[t][u - 2][w] : 0.0) + pc[1] * R[t][u - 1][w];
+                else r = (w > 1 ? (w - 1) * R[t][u][w - 2] : 0.0) + pc[2] * R[t][u][w - 1];
+                R[t][u][w] = r;
               }
+          R[0][0][0] = F[m] * fm2p[m];
+        }
         double da[3] = {0.0, 0.0, 0.0}, db[3] = {0.0, 0.0, 0.0};
+#pragma unroll
         for (int t = 0; t <= L; ++t)
+#pragma unroll
           for (int u = 0; u <= L - t; ++u)
+#pragma unroll
             for (int w = 0; w <= L - t - u; ++w) {
               const int h = (t * (L + 1) + u) * (L + 1) + w;
-              const double rr = R[0][t][u][w];
+              const double rr = R[t][u][w];
 #pragma unroll
               for (int d = 0; d < 3; ++d) {
                 da[d] += MA[d][h] * rr;
@@ -403,28 +470,33 @@ __device__ void one_pair_grad2(const OneParams &P, const double *Dm, const doubl
   }
 }
 
-// one CTA per ordered (a, b) index of the grid; the canonical ones (a >= b) work
+// one CTA per canonical pair (a >= b): block k = a (a + 1) / 2 + b
 __global__ void __launch_bounds__(kOneGradThreads) one_electron_grad_kernel(OneParams P, const double *D,
                                                                             const double *W, double *grad) {
-  const int a = blockIdx.x / P.nshell, b = blockIdx.x % P.nshell;
-  if (b > a) return;
+  const int k = blockIdx.x;
+  int a = (int)((sqrt(8.0 * k + 1.0) - 1.0) * 0.5);
+  while (a * (a + 1) / 2 > k) --a;
+  while ((a + 1) * (a + 2) / 2 <= k) ++a;
+  const int b = k - a * (a + 1) / 2;
+  __shared__ __align__(16) double smem[kOneGradSmem];
   switch (P.sh.l[a] * 3 + P.sh.l[b]) {
-    case 0: one_pair_grad2<0, 0>(P, D, W, grad, a, b); break;
-    case 1: one_pair_grad2<0, 1>(P, D, W, grad, a, b); break;
-    case 2: one_pair_grad2<0, 2>(P, D, W, grad, a, b); break;
-    case 3: one_pair_grad2<1, 0>(P, D, W, grad, a, b); break;
-    case 4: one_pair_grad2<1, 1>(P, D, W, grad, a, b); break;
-    case 5: one_pair_grad2<1, 2>(P, D, W, grad, a, b); break;
-    case 6: one_pair_grad2<2, 0>(P, D, W, grad, a, b); break;
-    case 7: one_pair_grad2<2, 1>(P, D, W, grad, a, b); break;
-    case 8: one_pair_grad2<2, 2>(P, D, W, grad, a, b); break;
+    case 0: one_pair_grad2<0, 0>(P, D, W, grad, a, b, smem); break;
+    case 1: one_pair_grad2<0, 1>(P, D, W, grad, a, b, smem); break;
+    case 2: one_pair_grad2<0, 2>(P, D, W, grad, a, b, smem); break;
+    case 3: one_pair_grad2<1, 0>(P, D, W, grad, a, b, smem); break;
+    case 4: one_pair_grad2<1, 1>(P, D, W, grad, a, b, smem); break;
+    case 5: one_pair_grad2<1, 2>(P, D, W, grad, a, b, smem); break;
+    case 6: one_pair_grad2<2, 0>(P, D, W, grad, a, b, smem); break;
+    case 7: one_pair_grad2<2, 1>(P, D, W, grad, a, b, smem); break;
+    case 8: one_pair_grad2<2, 2>(P, D, W, grad, a, b, smem); break;
     default: break;
   }
 }
 
 cudaError_t launch_one_electron_grad(const OneParams &P, const double *D, const double *W, double *grad,
                                      cudaStream_t st) {
-  const int n = P.nshell * P.nshell;
+  const int n = P.nshell * (P.nshell + 1) / 2;
+  if (n == 0) return cudaSuccess;
   one_electron_grad_kernel<<<n, kOneGradThreads, 0, st>>>(P, D, W, grad);
   return cudaGetLastError();
 }

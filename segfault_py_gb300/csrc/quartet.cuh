@@ -75,27 +75,35 @@ __device__ __forceinline__ dd shfl_up_r(unsigned m, dd v, int k) {
   return dd(__shfl_up_sync(m, v.hi, k), __shfl_up_sync(m, v.lo, k));
 }
 
-// Sums of v[0..N) over runs of equal key among the active lanes of a warp
-// (runs must be contiguous: consecutive quartets of a cost-sorted list share
-// their bra pair): segmented inclusive scan by shuffles; returns true on the
-// last lane of its run, which then holds the run's sums.  Lets one atomic per
-// run replace one per lane on addresses all lanes of the run share.
+// Sums of v[0..N) over runs of equal key among the active lanes of a warp: a
+// run is a maximal stretch of consecutive active lanes with one key (the
+// consecutive quartets of a list that share their bra pair).  The same key
+// may come back after a different one -- lists compacted on the device are
+// chunks of the cost-sorted list in any order -- and then starts a new run.
+// Segmented inclusive scan by shuffles, each lane taking partial sums only
+// from lanes at or after the head of its own run (a lane whose left
+// neighbour is inactive or has another key); returns true on the last lane of
+// its run, which then holds the run's sums.  Lets one atomic per run replace
+// one per lane on addresses all lanes of the run share.
 template <typename R, int N>
 __device__ __forceinline__ bool run_sums(int key, R (&v)[N]) {
   const unsigned mask = __activemask();
   const int lane = threadIdx.x & 31;
+  const int kl = __shfl_up_sync(mask, key, 1);
+  const bool head = lane == 0 || !((mask >> (lane - 1)) & 1u) || kl != key;
+  const unsigned heads = __ballot_sync(mask, head);
+  // highest head at or below this lane (the lowest active lane is a head)
+  const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const int k = __shfl_up_sync(mask, key, off);
-    const bool take = lane >= off && ((mask >> (lane - off)) & 1u) && k == key;
+    const bool take = lane - off >= start;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       const R o = shfl_up_r(mask, v[i], off);
       if (take) v[i] += o;
     }
   }
-  const int kn = __shfl_down_sync(mask, key, 1);
-  return lane == 31 || !((mask >> (lane + 1)) & 1u) || kn != key;
+  return lane == 31 || !((mask >> (lane + 1)) & 1u) || ((heads >> (lane + 1)) & 1u);
 }
 
 // 1/sqrt(a): single-precision hardware seed + two Newton-Raphson steps
@@ -1105,6 +1113,44 @@ __device__ __forceinline__ int64_t work_count(const ClassWork &w) {
 constexpr int kBlock = 128;
 constexpr int kMaxWsplit = 64;
 
+// One quartet group of the FP32 register path (one lane per quartet and
+// primitive sub-group): group gid of the list's W*P sub-groups per quartet,
+// Rys table rows read from the shared-memory copy tab_s of the class's root
+// block.  Returns false past the end of the list (nq quartets).  Used by the
+// class kernel's grid-stride loop and by the persistent multi-class kernel.
+template <int LA, int LB, int LC, int LD>
+__device__ __forceinline__ bool jk_f32_t1_step(const KParams &kp, const ClassWork &w, int64_t gid, int64_t nq,
+                                               const float *tab_s, const float *__restrict__ D, double *Jh,
+                                               double *Kh) {
+  using R = float;
+  const int P = w.psplit, W = w.wsplit;
+  const int p = threadIdx.x % P;
+  const int64_t q = gid / W;
+  if (q >= nq) return false;
+  const int sub = (int)(gid - q * W) * P + p;
+  const int2 ij = __ldg(w.list + q);
+  const QGeom<R> g = make_geom32(kp, w.x0 + ij.x, w.y0 + ij.y);
+  R scale = (R)1;
+  if (g.a == g.b) scale *= (R)0.5;
+  if (g.c == g.d) scale *= (R)0.5;
+  if (w.same && ij.x == ij.y) scale *= (R)0.5;
+  const int lane = threadIdx.x & 31;
+  const unsigned qmask = (P == 32) ? 0xffffffffu : (((1u << P) - 1u) << (lane & ~(P - 1)));
+  R acc[QC<LA, LB, LC, LD>::NABCD];
+  eval_t1<LA, LB, LC, LD, R>(kp, g, acc, sub, W * P, tab_s);
+  if (P > 1) reduce_psplit<R, QC<LA, LB, LC, LD>::NABCD, 1>(acc, P, qmask);
+  if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh, P == 1 ? ij.x : -1);
+  return true;
+}
+
+// copy the n-root block of the FP32 Rys table to shared memory (its rows are
+// read at lane-dependent intervals: divergent global loads)
+__device__ __forceinline__ void load_tab32_block(const KParams &kp, int nr, float4 *tab4) {
+  const int ntab4 = kTabNint * nr * kTab32Row / 4;
+  const float4 *src = reinterpret_cast<const float4 *>(kp.tab32 + rys_tab32v_offset(nr));
+  for (int k = threadIdx.x; k < ntab4; k += blockDim.x) tab4[k] = __ldg(src + k);
+}
+
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, const R *__restrict__ D, double *Jh,
                                                     double *Kh) {
@@ -1113,34 +1159,14 @@ __global__ void __launch_bounds__(kBlock) jk_kernel(KParams kp, ClassWork w, con
   const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
   if constexpr (T == 1 && std::is_same<R, float>::value) {
     // FP32 register path: the n-root block of the Rys table is copied to
-    // shared memory once per CTA (its rows are read at lane-dependent
-    // intervals: divergent global loads) and the CTA strides over the list
+    // shared memory once per CTA and the CTA strides over the list
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int NR = QC<LA, LB, LC, LD>::NR;
-    constexpr int NTAB4 = kTabNint * NR * kTab32Row / 4;
-    float4 *tab4 = reinterpret_cast<float4 *>(smem_raw);
-    const float4 *src = reinterpret_cast<const float4 *>(kp.tab32 + rys_tab32v_offset(NR));
-    for (int k = threadIdx.x; k < NTAB4; k += blockDim.x) tab4[k] = __ldg(src + k);
+    load_tab32_block(kp, QC<LA, LB, LC, LD>::NR, reinterpret_cast<float4 *>(smem_raw));
     __syncthreads();
     const float *tab_s = reinterpret_cast<const float *>(smem_raw);
     const int64_t nq = work_count(w);
-    for (int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;; gid += (int64_t)gridDim.x * (kBlock / TP)) {
-      const int64_t q = gid / W;
-      if (q >= nq) return;
-      const int sub = (int)(gid - q * W) * P + p;
-      const int2 ij = __ldg(w.list + q);
-      const QGeom<R> g = make_geom32(kp, w.x0 + ij.x, w.y0 + ij.y);
-      R scale = (R)1;
-      if (g.a == g.b) scale *= (R)0.5;
-      if (g.c == g.d) scale *= (R)0.5;
-      if (w.same && ij.x == ij.y) scale *= (R)0.5;
-      const int lane = threadIdx.x & 31;
-      const unsigned qmask = (TP == 32) ? 0xffffffffu : (((1u << TP) - 1u) << (lane & ~(TP - 1)));
-      R acc[QC<LA, LB, LC, LD>::NABCD];
-      eval_t1<LA, LB, LC, LD, R>(kp, g, acc, sub, W * P, tab_s);
-      if (P > 1) reduce_psplit<R, QC<LA, LB, LC, LD>::NABCD, 1>(acc, P, qmask);
-      if (p == 0) digest_t1<LA, LB, LC, LD, R>(kp, g, acc, scale, D, Jh, Kh, P == 1 ? ij.x : -1);
-    }
+    for (int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;; gid += (int64_t)gridDim.x * (kBlock / TP))
+      if (!jk_f32_t1_step<LA, LB, LC, LD>(kp, w, gid, nq, tab_s, D, Jh, Kh)) return;
   }
   const int64_t gid = (int64_t)blockIdx.x * (kBlock / TP) + grp;
   const int64_t q = gid / W;

@@ -110,15 +110,26 @@ class FockBuilder:
             _lib.check(_lib.lib().sf_schwarz(self._h, q.ctypes.data, _stream_ptr()))
         return q
 
-    def set_density_screening(self, on: bool = True, fock_fp32_cutoff: float = -1.0,
+    def set_density_screening(self, fock: bool = False, grad: bool = True, fock_fp32_cutoff: float = -1.0,
                               grad_drop_cutoff: float = -1.0, grad_fp32_cutoff: float = -1.0):
         """Density-weighted classification of every later Fock build and
-        gradient (sf_set_density_screening): the mixed modes run an
+        gradient (sf_set_density_screening).  ``fock``: the mixed modes run an
         accurate-tier quartet in FP32 when its density-weighted bound is below
-        the FP32 cutoff; the gradient leaves out quartets whose bound is below
-        the drop cutoff.  Negative cutoffs: the call's own."""
-        _lib.check(_lib.lib().sf_set_density_screening(self._h, 1 if on else 0, fock_fp32_cutoff,
+        the FP32 cutoff (off by default: the split then follows D between SCF
+        iterations and slows convergence).  ``grad``: the gradient leaves out
+        quartets whose bound is below the drop cutoff (on by default).
+        Negative cutoffs: the call's own."""
+        flags = (1 if fock else 0) | (2 if grad else 0)
+        _lib.check(_lib.lib().sf_set_density_screening(self._h, flags, fock_fp32_cutoff,
                                                        grad_drop_cutoff, grad_fp32_cutoff))
+
+    def set_launch_mode(self, mode: str = "streams", ctas_per_sm: int = 0):
+        """How Fock builds launch their class kernels (sf_set_launch_mode):
+        "streams" (one launch per class slice on 16 side streams) or
+        "persistent" (the FP32 register-path classes as one persistent launch
+        per register tier, fed by a device work queue)."""
+        m = {"streams": 0, "persistent": 1}[mode]
+        _lib.check(_lib.lib().sf_set_launch_mode(self._h, m, ctas_per_sm))
 
     def set_partition(self, part: int, nparts: int):
         _lib.check(_lib.lib().sf_set_partition(self._h, part, nparts))

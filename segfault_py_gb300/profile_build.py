@@ -85,6 +85,11 @@ def main(argv=None):
     ap.add_argument("--time", action="store_true",
                     help="also time --builds normal (concurrent) builds (or gradients) with events")
     ap.add_argument("--autotune", action="store_true", help="autotune the launch shapes first")
+    ap.add_argument("--launch", default="streams", choices=["streams", "persistent"],
+                    help="launch mode of the Fock build (sf_set_launch_mode)")
+    ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent grid: CTAs per SM (0: occupancy)")
+    ap.add_argument("--density", default="grad", choices=["none", "grad", "fock", "both"],
+                    help="density-weighted classification of the quartet lists (sf_set_density_screening)")
     ap.add_argument("--grad", action="store_true",
                     help="profile the two-electron gradient (sf_grad_jk) instead of the Fock build")
     ap.add_argument("--one-electron", action="store_true",
@@ -96,6 +101,8 @@ def main(argv=None):
     mol = Molecule.from_geometry(sym, xyz, a.basis)
     fb = FockBuilder(mol, cutoff=a.cutoff, fp32_cutoff=a.fp32_cutoff, precision=a.precision)
     D = guess_density(fb, mol.nelectron // 2)
+    fb.set_density_screening(fock=a.density in ("fock", "both"), grad=a.density in ("grad", "both"))
+    fb.set_launch_mode(a.launch, a.ctas_per_sm)
     if a.one_electron:
         from . import _lib
         from .fock import _ptr, _stream_ptr

@@ -1,6 +1,6 @@
 """Density-weighted classification of the quartet lists (sf_set_density_screening):
-the Fock build's mixed modes move accurate-tier quartets whose bound
-Q_ab Q_cd max|D| is below the FP32 cutoff to FP32, the gradient leaves out
+the Fock build's mixed modes (when switched on) move accurate-tier quartets whose
+bound Q_ab Q_cd max|D| is below the FP32 cutoff to FP32, the gradient leaves out
 quartets whose Q_ab Q_cd |Gamma| bound is below the Schwarz cutoff.  Checked
 against the same builds with the classification off."""
 import numpy as np
@@ -34,10 +34,11 @@ def _energy(fb, r, precision):
 def test_fock_demotion_keeps_energy(cuda, cluster, precision):
     mol, fb, r = cluster
     e64, _ = _energy(fb, r, "fp64")
-    fb.set_density_screening(False)
+    fb.set_density_screening(fock=False)
     e_off, st_off = _energy(fb, r, precision)
-    fb.set_density_screening(True)
+    fb.set_density_screening(fock=True)
     e_on, st_on = _energy(fb, r, precision)
+    fb.set_density_screening()
     # quartets move from the accurate tier to FP32, none is lost
     assert st_on["quartets_fp64"] < st_off["quartets_fp64"]
     assert st_on["quartets_fp64"] + st_on["quartets_fp32"] == st_off["quartets_fp64"] + st_off["quartets_fp32"]
@@ -49,9 +50,9 @@ def test_fock_demotion_keeps_energy(cuda, cluster, precision):
 def test_gradient_screening_matches_unscreened(cuda, cluster):
     from segfault_py_gb300.grad import rhf_gradient
     mol, fb, r = cluster
-    fb.set_density_screening(False)
+    fb.set_density_screening(grad=False)
     g_off = rhf_gradient(mol, r, fb, precision="fp64")
-    fb.set_density_screening(True)
+    fb.set_density_screening(grad=True)
     g_on = rhf_gradient(mol, r, fb, precision="fp64")
     g_mx = rhf_gradient(mol, r, fb, precision="mixed_df")
     assert float((g_on - g_off).abs().max()) < 1e-8
@@ -62,6 +63,7 @@ def test_graph_replay_reclassifies_a_new_density(cuda, cluster):
     """The classification is part of the captured build: a replay after D
     changed gives the eager result for the new D."""
     mol, fb, r = cluster
+    fb.set_density_screening(fock=True)
     D = r.D.contiguous().clone()
     J = torch.empty_like(D)
     K = torch.empty_like(D)
@@ -72,6 +74,7 @@ def test_graph_replay_reclassifies_a_new_density(cuda, cluster):
     g.replay()
     torch.cuda.synchronize()
     Je, Ke = fb.jk(D, precision="mixed_df")
+    fb.set_density_screening()
     scale = max(float(Je.abs().max()), float(Ke.abs().max()))
     assert float((J - Je).abs().max()) <= 1e-12 * scale
     assert float((K - Ke).abs().max()) <= 1e-12 * scale

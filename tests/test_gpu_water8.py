@@ -120,3 +120,67 @@ def test_water16_gradient_vs_fd_subset(cuda):
         fd = (energy(xp) - energy(xm)) / (2 * STEP)
         assert abs(fd - g64[a, d]) < 1e-6, ("fp64", a, d, fd, g64[a, d])
         assert abs(fd - gmx[a, d]) < 1e-6, ("mixed_df", a, d, fd, gmx[a, d])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_water8_fock_demotion_vs_oracle(cuda, w8, w8_gpu, precision):
+    """Density-weighted demotion of the accurate tier switched on: the lists
+    are compacted on the device (chunks in any order), the energy stays within
+    1e-6 Eh of the oracle and repeated builds agree to FP32 rounding."""
+    mol, fb = w8_gpu
+    D = torch.tensor(w8["D"], device=cuda)
+    fb.set_density_screening(fock=True)
+    try:
+        es = []
+        for _ in range(3):
+            J, K = fb.jk(D, precision=precision)
+            J, K = J.cpu().numpy(), K.cpu().numpy()
+            es.append(0.5 * float(np.sum(w8["D"] * (2.0 * w8["H"] + J - 0.5 * K))) + w8["e_nuc"])
+    finally:
+        fb.set_density_screening()
+    e_ref = w8["e_elec"] + w8["e_nuc"]
+    assert max(abs(e - e_ref) for e in es) < 1e-6, [e - e_ref for e in es]
+    # compacted lists come in a varying chunk order: the FP32 run sums round differently
+    assert max(es) - min(es) < 1e-8
+
+
+def test_water8_screened_gradient_deterministic(cuda, w8, w8_gpu):
+    """Gradient with the density screening (compacted lists): translationally
+    invariant and identical to rounding over repeated calls, FP64 and mixed."""
+    from segfault_py_gb300 import _lib
+    from segfault_py_gb300.fock import _ptr, _stream_ptr
+    mol, fb = w8_gpu
+    D = torch.tensor(w8["D"], device=cuda)
+    # FP32 per-CTA sums in shared memory add in a varying order: their
+    # rounding differs between calls
+    for prec, tol, rep in (("fp64", 1e-10, 1e-12), ("mixed_df", 1e-6, 1e-6)):
+        outs = []
+        for _ in range(4):
+            g = torch.zeros(3 * mol.natom, dtype=torch.float64, device=cuda)
+            _lib.check(_lib.lib().sf_grad_jk(fb.handle, _ptr(D), _ptr(g), _lib.PRECISION[prec], CUTOFF, FP32_CUTOFF,
+                                             _stream_ptr()))
+            outs.append(g.view(-1, 3).cpu().numpy())
+        for o in outs:
+            assert np.abs(o.sum(axis=0)).max() < tol, (prec, o.sum(axis=0))
+            assert np.abs(o - outs[0]).max() < rep, prec
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed", "mixed_df"])
+def test_water8_persistent_launch_matches_streams(cuda, w8, w8_gpu, precision):
+    """The FP32 register-path classes as persistent tier launches fed by a
+    device work queue: J/K equal to the stream launches' to FP32 rounding of
+    the summation order, energies within the mode's bound of the oracle."""
+    mol, fb = w8_gpu
+    D = torch.tensor(w8["D"], device=cuda)
+    J0, K0 = (x.cpu().numpy() for x in fb.jk(D, precision=precision))
+    fb.set_launch_mode("persistent")
+    try:
+        for _ in range(2):
+            J1, K1 = (x.cpu().numpy() for x in fb.jk(D, precision=precision))
+            assert np.abs(J1 - J0).max() <= 1e-9 * np.abs(J0).max()
+            assert np.abs(K1 - K0).max() <= 1e-9 * np.abs(K0).max()
+    finally:
+        fb.set_launch_mode("streams")
+    if precision != "fp32":
+        e = 0.5 * float(np.sum(w8["D"] * (2.0 * w8["H"] + J1 - 0.5 * K1))) + w8["e_nuc"]
+        assert abs(e - (w8["e_elec"] + w8["e_nuc"])) < 1e-6
