@@ -15,8 +15,10 @@ Reported:
                (256 MB write) before every step, each step timed by CUDA events;
                each build launched eagerly through FockBuilder.jk
                (graph_replay_value: the same build replayed from a CUDA graph;
-               persistent_launch_value: the FP32 register-path classes as one
-               persistent launch per register tier, fed by a device work queue)
+               graph_native_value: the library's own capture of the build,
+               replayed with node priorities; persistent_launch_value: the FP32
+               register-path classes as one persistent launch per register
+               tier, fed by a device work queue)
 * e2e          same metric through the public API with host buffers: pinned D
                -> device, Fock build, J and K -> pinned host, every step
 * fp64         the all-FP64 build, same protocol (the plain FP64 GPU baseline)
@@ -271,6 +273,10 @@ def run_ours(args):
     # the same build replayed from a captured CUDA graph, reported beside
     g_hl = fb.capture_jk(D, J, K, precision=HEADLINE)
     t_hl_graph = time_steps(g_hl.replay, args.steps, args.warmup, flush, stream)
+    # the library's own capture, replayed with the side streams' priorities
+    g_nat = fb.capture_jk(D, J, K, precision=HEADLINE, native=True)
+    t_hl_native = time_steps(g_nat.replay, args.steps, args.warmup, flush, stream)
+    g_nat.close()
     # the same build with the FP32 register-path classes as persistent tier
     # launches fed by a device work queue (sf_set_launch_mode), reported beside
     fb.set_launch_mode("persistent")
@@ -314,6 +320,8 @@ def run_ours(args):
     steps = args.steps
     value = world * steps / (ms_hl * 1e-3)
     peaks = fma_peaks(dev)
+    forces_roof = {prec: grad_roofline(fb, D, prec, peaks, max(3, steps // 4), args.warmup, flush, stream)
+                   for prec in (HEADLINE, "fp64")}
     # roofline of the dominant class kernel of the headline build (double-float
     # kernels run on the FP32 pipe: their FP64-equivalent algorithmic FLOPs are
     # set against the FP32 FMA peak)
@@ -354,6 +362,7 @@ def run_ours(args):
                             "energy_error_vs_fp64": emx - e64, "speedup_vs_fp64": ms_64 / ms_mx},
         "graph_replay_value": world * steps / (float(np.sum(t_hl_graph)) * 1e-3),
         "persistent_launch_value": world * steps / (float(np.sum(t_hl_persist)) * 1e-3),
+        "graph_native_value": world * steps / (float(np.sum(t_hl_native)) * 1e-3),
         "quartets_per_s": (st_hl["quartets_fp64"] + st_hl["quartets_fp32"]) * world * steps / (ms_hl * 1e-3),
         "prim_quartets_per_s": (st_hl["prim_quartets_fp64"] + st_hl["prim_quartets_fp32"]) * world * steps
                                / (ms_hl * 1e-3),
@@ -364,7 +373,8 @@ def run_ours(args):
         "forces": {"value": world * 1e3 / float(np.mean(t_f[HEADLINE])), "unit": "forces/s",
                    "fp64": world * 1e3 / float(np.mean(t_f["fp64"])),
                    "max_grad_error_mixed_vs_fp64": grad_err, "unit_error": "Eh/bohr",
-                   "note": "derivative integrals: FP32 below the cutoff, double-float above"},
+                   "note": "derivative integrals: FP32 below the cutoff, double-float above",
+                   "roofline": forces_roof},
         "autotune_s": tune_s,
         "setup": setup,
         "gpu_launches": (int(st_hl["launches"]) * 3 + int(st_64["launches"])) * steps,
@@ -388,6 +398,38 @@ def run_ours(args):
 
 
 # ----------------------------------------------------------------------------
+def grad_roofline(fb, D, precision, peaks, steps, warmup, flush, stream):
+    """Two-electron gradient (sf_grad_jk) alone: CUDA-event time per call and
+    the algorithmic FLOPs of its surviving derivative quartets (sf_grad_stats:
+    K_aK_bK_cK_d n' 36 N_c per quartet) against the FMA peak of the pipe each
+    tier runs on (FP32 pipe for FP32 and double-float, FP64 pipe for FP64)."""
+    import ctypes as C
+    import torch
+    from segfault_py_gb300 import _lib
+    from segfault_py_gb300.fock import _ptr, _stream_ptr
+    L = _lib.lib()
+    g = torch.zeros(3 * fb.mol.natom, dtype=torch.float64, device=D.device)
+
+    def run():
+        _lib.check(L.sf_grad_jk(fb.handle, _ptr(D), _ptr(g), _lib.PRECISION[precision], fb.cutoff, fb.fp32_cutoff,
+                                _stream_ptr()))
+    t = time_steps(run, steps, warmup, flush, stream)
+    st = _lib.Stats()
+    _lib.check(L.sf_grad_stats(fb.handle, C.byref(st), _stream_ptr()))
+    d = st.as_dict()
+    ms = float(np.mean(t))
+    acc_pipe = "fp64" if precision in ("fp64", "mixed") else "fp32"
+    t_acc = d["flop_alg_fp64"] / (peaks[acc_pipe] * 1e12)
+    t_32 = d["flop_alg_fp32"] / (peaks["fp32"] * 1e12)
+    return {"precision": precision, "two_electron_ms": ms, "launches": d["launches"],
+            "quartets_accurate": d["quartets_fp64"], "quartets_fp32": d["quartets_fp32"],
+            "flop_alg_accurate": d["flop_alg_fp64"], "flop_alg_fp32": d["flop_alg_fp32"],
+            "achieved_tflops": (d["flop_alg_fp64"] + d["flop_alg_fp32"]) / (ms * 1e-3) / 1e12,
+            "combined_frac": (t_acc + t_32) / (ms * 1e-3),
+            "unit": "TFLOP/s", "peak_source": "live FMA-chain kernel (sf_fma_peak), this run",
+            "flop_alg": "per surviving derivative quartet K_aK_bK_cK_d n' 36 N_c (n' = floor((L+1)/2)+1)"}
+
+
 ORACLE_FIXTURE = os.path.join(REPO, "tests", "golden", "water8_631gs.npz")
 
 

@@ -195,6 +195,25 @@ int sf_set_tuning(sf_handle *h, const sf_tune_entry *entries, int32_t n);
 int sf_set_density_screening(sf_handle *h, int32_t flags, double fock_fp32_cutoff, double grad_drop_cutoff,
                              double grad_fp32_cutoff);
 
+/* One Fock build captured as a CUDA graph, for callers that replay it (an SCF
+ * iteration on a fixed geometry): sf_fock_jk_graph_create runs one ordinary
+ * sf_fock_jk (which cuts and caches the quartet lists), then captures a
+ * second one on an internal stream (the class launches and their fork/join
+ * over the side streams become graph nodes) and instantiates it.  With
+ * node_priority != 0 the graph runs each launch at the priority of the side
+ * stream it was captured from (cudaGraphInstantiateFlagUseNodePriority): the
+ * accurate tier of a mixed build keeps its high priority, as in an eager
+ * build; with 0 every node runs at the priority of the launching stream.
+ * sf_fock_graph_launch replays it on a stream for the current contents of D
+ * (same pointers, same precision and cutoffs); nothing allocates.  Changing
+ * the handle's lists (sf_autotune, sf_set_tuning, sf_set_partition,
+ * sf_schwarz) invalidates the graph.  No counterpart in the reference. */
+typedef struct sf_fock_graph sf_fock_graph;
+int sf_fock_jk_graph_create(sf_handle *h, const double *D, double *J, double *K, int32_t precision, double cutoff,
+                            double fp32_cutoff, int32_t node_priority, void *stream, sf_fock_graph **out);
+int sf_fock_graph_launch(sf_fock_graph *g, void *stream);
+void sf_fock_graph_destroy(sf_fock_graph *g);
+
 /* How a Fock build launches its class kernels (no counterpart in the
  * reference, whose scheduler is Pool(8).map over AO quartets, hf.py:45-47):
  *  - SF_LAUNCH_STREAMS (default): one launch per (class, precision, primitive
@@ -252,6 +271,16 @@ int sf_eri_plan_run(sf_eri_plan *plan, int32_t precision, double *out, void *str
  * FP32 accuracy); synchronises the stream and returns SF_ECUDA if a bounded
  * wait on the tensor cores timed out.  Other precisions: SF_EUNSUPPORTED. */
 int sf_eri_plan_run_md(sf_eri_plan *plan, int32_t precision, double *out, void *stream);
+/* Test hook for the error path of the tensor-core McMurchie-Davidson kernels
+ * (sf_eri_plan_run_md in FP32): every wait for their MMAs is bounded, and a
+ * wait that runs out sets a device flag, waits (again bounded) for the MMAs
+ * in flight, frees the tensor memory and returns; the run then fails with
+ * SF_ECUDA and its outputs are not to be used.  This sets the bound of the
+ * first wait to `iterations` polls: 0 makes it count as run out before its
+ * first poll, so a test can take that path without any fault; -1 restores
+ * the default (2^24 polls).  Process-wide; not for production use.  No
+ * counterpart in the reference. */
+int sf_debug_tc_wait_limit(int32_t iterations);
 void sf_eri_plan_destroy(sf_eri_plan *plan);
 
 /* One-electron matrices (device, nao*nao each): overlap S, kinetic T and
@@ -271,6 +300,17 @@ int sf_one_electron(sf_handle *h, const double *atom_xyz, const double *charges,
  * used by the shells) is accumulated, not zeroed. */
 int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, double cutoff,
                double fp32_cutoff, void *stream);
+
+/* Counters of the last sf_grad_jk call on this handle, after the
+ * density-weighted screening (synchronises `stream` first): surviving
+ * quartets and primitive quartets of the accurate tier ("fp64": FP64 or
+ * double-float) and of the FP32 tier, and their algorithmic FLOPs for
+ * derivative quartets, per quartet K_aK_bK_cK_d n' 36 N_c (nine derivative
+ * components, centres A, B, C times x, y, z, each a 4-FLOP assembly
+ * Ix' Iy Iz w per output, root and primitive quartet; n' = floor((L+1)/2)+1
+ * roots; root, recurrence and contraction work excluded); launches = the
+ * call's class launches.  No counterpart in the reference. */
+int sf_grad_stats(sf_handle *h, sf_stats *stats, void *stream);
 
 /* One-electron part of the gradient: derivatives of sum_pq D_pq (T+V)_pq
  * - W_pq S_pq with respect to the basis centres and, for V, the nuclei

@@ -24,7 +24,8 @@ EXPORTS = ["sf_version", "sf_last_error", "sf_create", "sf_build_shells", "sf_de
            "sf_fma_peak", "sf_fock_jk_noalloc", "sf_grad_jk", "sf_grad_one_electron",
            "sf_small_solve", "sf_eri_plan_create", "sf_eri_plan_info", "sf_eri_plan_offsets", "sf_eri_plan_run",
            "sf_eri_plan_destroy", "sf_autotune", "sf_tuning_count", "sf_get_tuning", "sf_set_tuning", "sf_eri_plan_run_md",
-           "sf_set_density_screening", "sf_set_launch_mode"]
+           "sf_set_density_screening", "sf_set_launch_mode", "sf_fock_jk_graph_create", "sf_fock_graph_launch",
+           "sf_fock_graph_destroy", "sf_debug_tc_wait_limit", "sf_grad_stats"]
 
 
 class SegFockUnavailable(ImportError):
@@ -123,6 +124,12 @@ def lib():
     L.sf_set_tuning.argtypes = [p, p, i32]
     L.sf_set_density_screening.argtypes = [p, i32, d, d, d]
     L.sf_set_launch_mode.argtypes = [p, i32, i32]
+    L.sf_fock_jk_graph_create.argtypes = [p, p, p, p, i32, d, d, i32, p, p]
+    L.sf_fock_graph_launch.argtypes = [p, p]
+    L.sf_fock_graph_destroy.argtypes = [p]
+    L.sf_fock_graph_destroy.restype = None
+    L.sf_debug_tc_wait_limit.argtypes = [i32]
+    L.sf_grad_stats.argtypes = [p, p, p]
     _lib = L
     return L
 

@@ -379,8 +379,10 @@ struct sf_handle {
   };
   std::vector<Launch> plan;
   bool plan_counts = false;                // quartet counts of the plan live on the device
+  bool plan_grad = false;                  // the last plan was a gradient's
   // launch mode SF_LAUNCH_PERSISTENT: the FP32 register-path lists of a Fock
   // build run as one persistent launch per register tier (jk_persist.cu)
+  cudaStream_t cap_st = nullptr;           // stream that sf_fock_jk_graph_create captures on
   int launch_mode = SF_LAUNCH_STREAMS;
   int persist_ctas_per_sm = 0;             // 0: the occupancy limit of each tier kernel
   int lists_version = 0, persist_version = -1;
@@ -828,6 +830,7 @@ int build_persist(sf_handle *h) {
 int make_plan(sf_handle *h, bool grad, int active) {
   h->plan.clear();
   h->pplan.clear();
+  h->plan_grad = grad;
   const bool persist = h->launch_mode == SF_LAUNCH_PERSISTENT && !grad && h->profiling == 0;
   if (persist && h->persist_version != h->lists_version) {
     const int rc = build_persist(h);
@@ -1018,10 +1021,14 @@ int convert_density(sf_handle *h, const double *D, float *D32, cudaStream_t st, 
 // work counters of the last plan: the host counts of the lists, or, when the
 // lists were classified on the device, the device counts (the stream must be
 // synchronised)
-int plan_stats(sf_handle *h, sf_stats *stats) {
+// grad: the algorithmic FLOPs of derivative quartets instead, per surviving
+// quartet K_aK_bK_cK_d n' 36 N_c (nine derivative components -- centres A,
+// B, C times x, y, z -- each a 4-FLOP assembly Ix' Iy Iz w per output, root
+// and primitive quartet; n' = floor((L+1)/2) + 1 roots)
+int plan_stats(sf_handle *h, sf_stats *stats, bool grad = false) {
   stats->quartets_total = h->st_total;
   stats->reserved = 0;
-  if (!h->plan_counts) {
+  if (!h->plan_counts && !grad) {
     stats->quartets_fp64 = h->st_q[0];
     stats->quartets_fp32 = h->st_q[1];
     stats->prim_quartets_fp64 = h->st_pq[0];
@@ -1031,13 +1038,15 @@ int plan_stats(sf_handle *h, sf_stats *stats) {
     return SF_OK;
   }
   std::vector<unsigned long long> c(4 * h->slices.size());
-  SF_CK(cudaMemcpy(c.data(), h->d_cnt.p, c.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  if (h->plan_counts)
+    SF_CK(cudaMemcpy(c.data(), h->d_cnt.p, c.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   int64_t q[2] = {0, 0}, pq[2] = {0, 0};
   double f[2] = {0.0, 0.0};
   for (const auto &L : h->plan) {
     const auto &sl = h->slices[L.slice];
     const ClassInfo &ci = kClassInfo[sl.cls];
-    const double nr = (ci.la + ci.lb + ci.lc + ci.ld) / 2 + 1;
+    const int lsum = ci.la + ci.lb + ci.lc + ci.ld;
+    const double nr = grad ? (lsum + 1) / 2 + 1 : lsum / 2 + 1;
     const double nabcd = (double)ncart(ci.la) * ncart(ci.lb) * ncart(ci.lc) * ncart(ci.ld);
     int64_t nq = sl.quartets, np = sl.prims;
     if (L.w.count) {
@@ -1048,7 +1057,7 @@ int plan_stats(sf_handle *h, sf_stats *stats) {
     const int t = L.kind == 1 ? 1 : 0;
     q[t] += nq;
     pq[t] += np;
-    f[t] += (double)np * nr * 4.0 * nabcd + 12.0 * nabcd * (double)nq;
+    f[t] += grad ? (double)np * nr * 36.0 * nabcd : (double)np * nr * 4.0 * nabcd + 12.0 * nabcd * (double)nq;
   }
   stats->quartets_fp64 = q[0];
   stats->quartets_fp32 = q[1];
@@ -1407,6 +1416,7 @@ void sf_destroy(sf_handle *h) {
     if (h->join_ev[k]) cudaEventDestroy(h->join_ev[k]);
   }
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->cap_st) cudaStreamDestroy(h->cap_st);
   delete h;
 }
 
@@ -1576,6 +1586,62 @@ int sf_fock_jk(sf_handle *h, const double *D, double *J, double *K, int32_t prec
     stats->launches = launches;
   }
   return SF_OK;
+}
+
+struct sf_fock_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int device = 0;
+};
+
+int sf_fock_jk_graph_create(sf_handle *h, const double *D, double *J, double *K, int32_t precision, double cutoff,
+                            double fp32_cutoff, int32_t node_priority, void *stream, sf_fock_graph **out) {
+  if (!out) return fail(SF_EINVAL, "sf_fock_jk_graph_create: out is NULL");
+  *out = nullptr;
+  if (!h) return fail(SF_EINVAL, "sf_fock_jk_graph_create: NULL handle");
+  // one ordinary build first: it cuts the quartet lists (and the persistent
+  // tile tables), which allocates -- nothing allocates inside the capture
+  int rc = sf_fock_jk(h, D, J, K, precision, cutoff, fp32_cutoff, nullptr, stream);
+  if (rc) return rc;
+  DeviceGuard g(h->device);
+  SF_CK(cudaStreamSynchronize((cudaStream_t)stream));
+  if (!h->cap_st) SF_CK(cudaStreamCreateWithFlags(&h->cap_st, cudaStreamNonBlocking));
+  SF_CK(cudaStreamBeginCapture(h->cap_st, cudaStreamCaptureModeThreadLocal));
+  rc = sf_fock_jk(h, D, J, K, precision, cutoff, fp32_cutoff, nullptr, h->cap_st);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(h->cap_st, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(SF_ECUDA, std::string("sf_fock_jk_graph_create: ") + cudaGetErrorString(e));
+  auto *fg = new sf_fock_graph;
+  fg->graph = graph;
+  fg->device = h->device;
+  const cudaError_t ei =
+      cudaGraphInstantiateWithFlags(&fg->exec, graph, node_priority ? cudaGraphInstantiateFlagUseNodePriority : 0);
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    delete fg;
+    return fail(SF_ECUDA, std::string("sf_fock_jk_graph_create: ") + cudaGetErrorString(ei));
+  }
+  *out = fg;
+  return SF_OK;
+}
+
+int sf_fock_graph_launch(sf_fock_graph *g, void *stream) {
+  if (!g || !g->exec) return fail(SF_EINVAL, "sf_fock_graph_launch: NULL graph");
+  DeviceGuard dg(g->device);
+  SF_CK(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  return SF_OK;
+}
+
+void sf_fock_graph_destroy(sf_fock_graph *g) {
+  if (!g) return;
+  DeviceGuard dg(g->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
 }
 
 int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff, double fp32_cutoff, int32_t reps,
@@ -1862,6 +1928,17 @@ int sf_grad_jk(sf_handle *h, const double *D, double *grad, int32_t precision, d
   return run_call(h, true, D, h->d_D32.p, nullptr, nullptr, grad, cutoff, fp32_cutoff, st, h->profiling, nullptr);
 }
 
+int sf_grad_stats(sf_handle *h, sf_stats *stats, void *stream) {
+  if (!h || !stats) return fail(SF_EINVAL, "sf_grad_stats: NULL argument");
+  if (!h->plan_grad || h->plan.empty()) return fail(SF_ESTATE, "sf_grad_stats: no gradient call on this handle yet");
+  DeviceGuard g(h->device);
+  SF_CK(cudaStreamSynchronize((cudaStream_t)stream));
+  const int rc = plan_stats(h, stats, true);
+  if (rc) return rc;
+  stats->launches = (int32_t)h->plan.size();
+  return SF_OK;
+}
+
 int sf_grad_one_electron(sf_handle *h, const double *atom_xyz, const double *charges, int32_t natom, const double *D,
                          const double *W, double *grad, void *stream) {
   if (!h) return fail(SF_EINVAL, "sf_grad_one_electron: NULL handle");
@@ -1971,6 +2048,12 @@ int sf_eri_plan_run_md(sf_eri_plan *pl, int32_t precision, double *out, void *st
   SF_CK(cudaMemcpyAsync(&flag, h->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   SF_CK(cudaStreamSynchronize(st));
   if (flag) return fail(SF_ECUDA, "sf_eri_plan_run_md: a tensor-core MMA wait timed out");
+  return SF_OK;
+}
+
+int sf_debug_tc_wait_limit(int32_t iterations) {
+  if (iterations < -1) return fail(SF_EINVAL, "sf_debug_tc_wait_limit: limit below -1");
+  md_tc_set_wait_limit(iterations);
   return SF_OK;
 }
 

@@ -35,6 +35,9 @@ cudaError_t prepare_md();
 // the same with the bra E contraction on the tensor cores (FP32 MD, 3-pass TF32)
 cudaError_t launch_md_tc(int cls, const KParams &kp, const EriWork &w, int nsm, cudaStream_t st);
 cudaError_t prepare_md_tc();
+// polls of md_tc's bounded MMA waits (0: out before the first poll, < 0: the
+// default); a test hook
+void md_tc_set_wait_limit(int iterations);
 // Schwarz bounds of pair class pc (0..5) over pairs [p0, p0+n)
 cudaError_t launch_schwarz(int pc, const KParams &kp, int p0, int n, double *qout, cudaStream_t st);
 

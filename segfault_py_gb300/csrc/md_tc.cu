@@ -113,7 +113,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }  // namespace
 
 template <int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(kTcThreads) md_tc_kernel(KParams kp, EriWork w) {
+__global__ void __launch_bounds__(kTcThreads) md_tc_kernel(KParams kp, EriWork w, int wait_limit) {
   using Q = QC<LA, LB, LC, LD>;
   constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
   constexpr int NHAB = nherm(LAB), NHL = nherm(L);
@@ -273,10 +273,9 @@ __global__ void __launch_bounds__(kTcThreads) md_tc_kernel(KParams kp, EriWork w
         mma_commit(mbar);
       }
       // every thread waits (bounded) for the MMAs before the operands are rewritten
-      int it = 0;
-      while (!mbar_try_wait(mbar, phase) && ++it < kMaxWait) {
-      }
-      if (it >= kMaxWait) {
+      bool done = false;
+      for (int it = 0; it < wait_limit && !done; ++it) done = mbar_try_wait(mbar, phase);
+      if (!done) {
         atomicExch(abort_flag, 1);
         if (kp.err) atomicExch(kp.err, 2);
       }
@@ -335,11 +334,20 @@ constexpr size_t md_tc_smem() {
   return 2 * kABytes + 2 * kBBytes + (2 * nherm(LA + LB + LC + LD) + 2) * sizeof(float) + 32;
 }
 
+// polls of the bounded wait on each MMA commit: kMaxWait unless a test
+// shortens it to make the wait run out (0: out before the first poll); the
+// wait after a timeout, which drains the MMAs before the tensor memory is
+// freed, always allows kMaxWait
+static int g_wait_limit = kMaxWait;
+
+void md_tc_set_wait_limit(int iterations) { g_wait_limit = iterations >= 0 ? iterations : kMaxWait; }
+
 template <int LA, int LB, int LC, int LD>
 static cudaError_t run_md_tc(const KParams &kp, const EriWork &w, int nsm, cudaStream_t st) {
   if (w.n <= 0) return cudaSuccess;
   const int64_t grid = std::min<int64_t>(w.n, (int64_t)std::max(nsm, 1) * 2);
-  md_tc_kernel<LA, LB, LC, LD><<<(unsigned)grid, kTcThreads, md_tc_smem<LA, LB, LC, LD>(), st>>>(kp, w);
+  md_tc_kernel<LA, LB, LC, LD><<<(unsigned)grid, kTcThreads, md_tc_smem<LA, LB, LC, LD>(), st>>>(kp, w,
+                                                                                                  g_wait_limit);
   return cudaGetLastError();
 }
 

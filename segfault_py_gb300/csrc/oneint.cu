@@ -2,8 +2,8 @@
 //
 // Reference: src/hf/mmd2.py:14-84 (Fortran E coefficients per primitive pair)
 // and src/hf/mmd.py:13-141, called per AO pair and per nucleus at
-// src/hf/hf.py:266-274.  Here one thread evaluates the whole Cartesian block
-// of one ordered shell pair (a, b):
+// src/hf/hf.py:266-274.  Here one CTA evaluates the whole Cartesian block of
+// one canonical shell pair (a >= b) and writes it and its transpose:
 //   E^{ij}_t  Hermite expansion coefficients (McMurchie-Davidson), built by
 //             the two-term recursions in i and j (mmd.py:13-30 in closed form:
 //             E^{i+1,j}_t = E^{ij}_{t-1}/(2p) + X_PA E^{ij}_t + (t+1) E^{ij}_{t+1})
@@ -70,130 +70,205 @@ __device__ __forceinline__ void hermite_e(double p, double xpa, double xpb, doub
 }
 
 
+// One CTA (kOneThreads threads) per canonical shell pair (a >= b); the
+// block of (a, b) is written, and for a != b also its transpose as the block
+// of (b, a) (S, T and V are symmetric).  Per primitive pair:
+//  * E coefficients along x, y, z (bra to LA, ket to LB+2 for the kinetic
+//    shifts) into shared memory, one direction per thread;
+//  * S and T of Cartesian entry (i, j) on thread i*NB + j;
+//  * V = 2 pi / p c_i c_j sum_tuv E E E S_tuv with S_tuv = sum_C -Z_C R_tuv
+//    (V is linear in R): every thread takes nuclei C = t, t+kOneThreads, ...,
+//    Boys values, R_tuv by the Hermite Coulomb recursion in place (level n
+//    overwrites t+u+v = L-n .. 1 from the top down, then R^n_000) and adds
+//    -Z_C R_tuv to its part of S_tuv; S is summed over the CTA (shuffles,
+//    then the two warps) and thread i*NB + j contracts it with its E's.
+// Primitive pairs whose contributions all stay below 1e-17 are skipped (the
+// product Gaussian c_i c_j exp(-mu |AB|^2) (pi/p)^3/2 bounds the overlap,
+// E coefficients grow at most as (|AB| + 1/sqrt(p) + 1)^L, kinetic terms as
+// 3 beta (LB + 2) and attraction as 2 sqrt(p/pi) times the summed charge).
+constexpr int kOneThreads = 64;
+
+// Hermite triples t+u+v <= L, enumerated t, then u, then v ascending
+__host__ __device__ constexpr int ntuv(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
+__host__ __device__ constexpr int tuv_index(int L, int t, int u, int v) {
+  int k = 0;
+  for (int t2 = 0; t2 < t; ++t2) k += (L - t2 + 1) * (L - t2 + 2) / 2;
+  for (int u2 = 0; u2 < u; ++u2) k += L - t - u2 + 1;
+  return k + v;
+}
+
 template <int LA, int LB>
-__device__ void one_pair(const OneParams &P, int a, int b) {
-  constexpr int NA = ncart(LA), NB = ncart(LB);
+constexpr int one_smem() {
+  return 3 * (LA + 1) * (LB + 3) * (LA + LB + 3) + 2 * ntuv(LA + LB) + 2;
+}
+constexpr int kOneSmem = one_smem<2, 2>();   // the largest
+
+template <int LA, int LB>
+__device__ void one_pair(const OneParams &P, int a, int b, double *smem) {
+  constexpr int NA = ncart(LA), NB = ncart(LB), L = LA + LB;
+  constexpr int EN = (LA + 1) * (LB + 3) * (LA + LB + 3);
+  using EArr = double[LA + 1][LB + 3][LA + LB + 3];
+  EArr *E = reinterpret_cast<EArr *>(smem);
+  constexpr int NT = ntuv(L);
+  double *sred = smem + 3 * EN;              // [2 warps][NT]: S_tuv partial sums
+  double *zred = smem + 3 * EN + 2 * NT;
+  static_assert(3 * EN + 2 * NT + 2 == one_smem<LA, LB>(), "smem layout");
+  const double pi = 3.14159265358979323846;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const double A[3] = {P.sh.cx[a], P.sh.cy[a], P.sh.cz[a]};
   const double B[3] = {P.sh.cx[b], P.sh.cy[b], P.sh.cz[b]};
-  double s[NA][NB], k[NA][NB], v[NA][NB];
-#pragma unroll
-  for (int i = 0; i < NA; ++i)
-#pragma unroll
-    for (int j = 0; j < NB; ++j) s[i][j] = k[i][j] = v[i][j] = 0.0;
-  const double pi = 3.14159265358979323846;
-  for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia) {
+  double R2 = 0.0;
+  for (int d = 0; d < 3; ++d) R2 += (A[d] - B[d]) * (A[d] - B[d]);
+  double zs = 0.0;
+  if (P.V)
+    for (int k = tid; k < P.natom; k += blockDim.x) zs += fabs(P.charges[k]);
+  for (int off = 16; off > 0; off >>= 1) zs += __shfl_xor_sync(0xffffffffu, zs, off);
+  if (lane == 0) zred[warp] = zs;
+  __syncthreads();
+  zs = zred[0] + zred[1];
+  const int ti = tid / NB, tj = tid % NB;   // this thread's S/T entry (tid < NA*NB)
+  double s_acc = 0.0, t_acc = 0.0, v_acc = 0.0;
+  for (int ia = P.poff[a]; ia < P.poff[a + 1]; ++ia)
     for (int ib = P.poff[b]; ib < P.poff[b + 1]; ++ib) {
       const double al = P.exps[ia], be = P.exps[ib], p = al + be, mu = al * be / p;
       const double cc = P.coefs[ia] * P.coefs[ib];
-      double Pc[3], E[3][LA + 1][LB + 3][LA + LB + 3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        Pc[d] = (al * A[d] + be * B[d]) / p;
-        const double X = A[d] - B[d];
-        hermite_e<LA, LB + 2>(p, Pc[d] - A[d], Pc[d] - B[d], exp(-mu * X * X), E[d]);
-      }
       const double sp = pow(pi / p, 1.5);
-      // overlap and kinetic
+      {
+        const double g = fabs(cc) * exp(-mu * R2) * sp;
+        const double e = pow(sqrt(R2) + rsqrt(p) + 1.0, (double)L);
+        const double f = 1.0 + 2.0 * sqrt(p / pi) * zs + 3.0 * be * (LB + 2);
+        if (g * e * f < 1e-17) continue;   // uniform over the CTA
+      }
+      double Pc[3];
+      for (int d = 0; d < 3; ++d) Pc[d] = (al * A[d] + be * B[d]) / p;
+      __syncthreads();   // previous iteration done with E
+      if (tid < 3) {
+        const int d = tid;
+        const double X = A[d] - B[d];
+        double Et[LA + 1][LB + 3][LA + LB + 3];
+        hermite_e<LA, LB + 2>(p, Pc[d] - A[d], Pc[d] - B[d], exp(-mu * X * X), Et);
+        for (int i = 0; i <= LA; ++i)
+          for (int j = 0; j <= LB + 2; ++j)
+            for (int t = 0; t <= LA + LB + 2; ++t) E[d][i][j][t] = Et[i][j][t];
+      }
+      __syncthreads();
+      if (tid < NA * NB) {   // overlap and kinetic
+        const int ax = cart_e(LA, ti, 0), ay = cart_e(LA, ti, 1), az = cart_e(LA, ti, 2);
+        const int bx = cart_e(LB, tj, 0), by = cart_e(LB, tj, 1), bz = cart_e(LB, tj, 2);
+        const double sx = E[0][ax][bx][0], sy = E[1][ay][by][0], sz = E[2][az][bz][0];
+        const double s0 = sx * sy * sz * sp;
+        double t = be * (2 * (bx + by + bz) + 3) * s0;
+        t -= 2.0 * be * be * sp *
+             (E[0][ax][bx + 2][0] * sy * sz + sx * E[1][ay][by + 2][0] * sz + sx * sy * E[2][az][bz + 2][0]);
+        if (bx >= 2) t -= 0.5 * bx * (bx - 1) * sp * E[0][ax][bx - 2][0] * sy * sz;
+        if (by >= 2) t -= 0.5 * by * (by - 1) * sp * sx * E[1][ay][by - 2][0] * sz;
+        if (bz >= 2) t -= 0.5 * bz * (bz - 1) * sp * sx * sy * E[2][az][bz - 2][0];
+        s_acc += cc * s0;
+        t_acc += cc * t;
+      }
+      if (P.V) {   // nuclear attraction, nuclei across threads
+        double st[NT];
 #pragma unroll
-      for (int i = 0; i < NA; ++i)
-#pragma unroll
-        for (int j = 0; j < NB; ++j) {
-          const int ax = cart_e(LA, i, 0), ay = cart_e(LA, i, 1), az = cart_e(LA, i, 2);
-          const int bx = cart_e(LB, j, 0), by = cart_e(LB, j, 1), bz = cart_e(LB, j, 2);
-          const double sx = E[0][ax][bx][0], sy = E[1][ay][by][0], sz = E[2][az][bz][0];
-          const double s0 = sx * sy * sz * sp;
-          double t = be * (2 * (bx + by + bz) + 3) * s0;
-          t -= 2.0 * be * be * sp * (E[0][ax][bx + 2][0] * sy * sz + sx * E[1][ay][by + 2][0] * sz + sx * sy * E[2][az][bz + 2][0]);
-          if (bx >= 2) t -= 0.5 * bx * (bx - 1) * sp * E[0][ax][bx - 2][0] * sy * sz;
-          if (by >= 2) t -= 0.5 * by * (by - 1) * sp * sx * E[1][ay][by - 2][0] * sz;
-          if (bz >= 2) t -= 0.5 * bz * (bz - 1) * sp * sx * sy * E[2][az][bz - 2][0];
-          s[i][j] += cc * s0;
-          k[i][j] += cc * t;
-        }
-      // nuclear attraction
-      if (P.V) {
-        for (int at = 0; at < P.natom; ++at) {
-          const double Cc[3] = {P.atom_xyz[3 * at], P.atom_xyz[3 * at + 1], P.atom_xyz[3 * at + 2]};
-          const double pc[3] = {Pc[0] - Cc[0], Pc[1] - Cc[1], Pc[2] - Cc[2]};
-          const double Tb = p * (pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
-          constexpr int L = LA + LB;
+        for (int k = 0; k < NT; ++k) st[k] = 0.0;
+        for (int at = tid; at < P.natom; at += blockDim.x) {
+          const double pc[3] = {Pc[0] - P.atom_xyz[3 * at], Pc[1] - P.atom_xyz[3 * at + 1],
+                                Pc[2] - P.atom_xyz[3 * at + 2]};
           double F[L + 1];
-          boys_array(L, Tb, F);
-          // R^n_{tuv} bottom-up: R[n][t][u][v] for t+u+v <= L-n
-          double R[L + 1][L + 1][L + 1][L + 1];
-          for (int n = 0; n <= L; ++n) {
-            double f = F[n];
-            for (int m = 0; m < n; ++m) f *= -2.0 * p;
-            R[n][0][0][0] = f;
-          }
+          boys_array(L, p * (pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]), F);
+          double R[L + 1][L + 1][L + 1];
+          double fm2p = 1.0;
+#pragma unroll
+          for (int n = 0; n < L; ++n) fm2p *= -2.0 * p;
+          R[0][0][0] = F[L] * fm2p;
+#pragma unroll
           for (int n = L - 1; n >= 0; --n) {
-            for (int t = 0; t <= L - n; ++t)
-              for (int u = 0; u <= L - n - t; ++u)
-                for (int w = 0; w <= L - n - t - u; ++w) {
-                  if (t + u + w == 0) continue;
+#pragma unroll
+            for (int sl = L - n; sl >= 1; --sl)
+#pragma unroll
+              for (int t = 0; t <= sl; ++t)
+#pragma unroll
+                for (int u = 0; u <= sl - t; ++u) {
+                  const int w = sl - t - u;
                   double r;
-                  if (t > 0) r = (t > 1 ? (t - 1) * R[n + 1][t - 2][u][w] : 0.0) + pc[0] * R[n + 1][t - 1][u][w];
-                  else if (u > 0) r = (u > 1 ? (u - 1) * R[n + 1][t][u - 2][w] : 0.0) + pc[1] * R[n + 1][t][u - 1][w];
-                  else r = (w > 1 ? (w - 1) * R[n + 1][t][u][w - 2] : 0.0) + pc[2] * R[n + 1][t][u][w - 1];
-                  R[n][t][u][w] = r;
+                  if (t > 0) r = (t > 1 ? (t - 1) * R[t - 2][u][w] : 0.0) + pc[0] * R[t - 1][u][w];
+                  else if (u > 0) r = (u > 1 ? (u - 1) * R[t][u - 2][w] : 0.0) + pc[1] * R[t][u - 1][w];
+                  else r = (w > 1 ? (w - 1) * R[t][u][w - 2] : 0.0) + pc[2] * R[t][u][w - 1];
+                  R[t][u][w] = r;
                 }
+            fm2p /= -2.0 * p;
+            R[0][0][0] = F[n] * fm2p;
           }
-          const double pre = -P.charges[at] * 2.0 * pi / p;
+          const double z = -P.charges[at];
 #pragma unroll
-          for (int i = 0; i < NA; ++i)
+          for (int t = 0; t <= L; ++t)
 #pragma unroll
-            for (int j = 0; j < NB; ++j) {
-              const int ax = cart_e(LA, i, 0), ay = cart_e(LA, i, 1), az = cart_e(LA, i, 2);
-              const int bx = cart_e(LB, j, 0), by = cart_e(LB, j, 1), bz = cart_e(LB, j, 2);
-              double acc = 0.0;
+            for (int u = 0; u <= L - t; ++u)
 #pragma unroll
-              for (int t = 0; t <= ax + bx; ++t)
+              for (int w = 0; w <= L - t - u; ++w) st[tuv_index(L, t, u, w)] += z * R[t][u][w];
+        }
 #pragma unroll
-                for (int u = 0; u <= ay + by; ++u)
-#pragma unroll
-                  for (int w = 0; w <= az + bz; ++w)
-                    acc += E[0][ax][bx][t] * E[1][ay][by][u] * E[2][az][bz][w] * R[0][t][u][w];
-              v[i][j] += cc * pre * acc;
-            }
+        for (int k = 0; k < NT; ++k) {
+          double x = st[k];
+          for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+          if (lane == 0) sred[warp * NT + k] = x;
+        }
+        __syncthreads();
+        if (tid < NA * NB) {
+          const int ax = cart_e(LA, ti, 0), ay = cart_e(LA, ti, 1), az = cart_e(LA, ti, 2);
+          const int bx = cart_e(LB, tj, 0), by = cart_e(LB, tj, 1), bz = cart_e(LB, tj, 2);
+          double acc = 0.0;
+          for (int t = 0; t <= ax + bx; ++t)
+            for (int u = 0; u <= ay + by; ++u)
+              for (int w = 0; w <= az + bz; ++w) {
+                const int k = tuv_index(L, t, u, w);
+                acc += E[0][ax][bx][t] * E[1][ay][by][u] * E[2][az][bz][w] * (sred[k] + sred[NT + k]);
+              }
+          v_acc += 2.0 * pi / p * cc * acc;
         }
       }
+    }
+  if (tid < NA * NB) {
+    const int a0 = P.sh.ao[a], b0 = P.sh.ao[b], n = P.nao;
+    const double nrm = cart_norm(LA, ti) * cart_norm(LB, tj);
+    const size_t ij = (size_t)(a0 + ti) * n + b0 + tj, ji = (size_t)(b0 + tj) * n + a0 + ti;
+    const double vv = v_acc * nrm;
+    if (P.S) P.S[ij] = s_acc * nrm;
+    if (P.T) P.T[ij] = t_acc * nrm;
+    if (P.V) P.V[ij] = vv;
+    if (a != b) {
+      if (P.S) P.S[ji] = s_acc * nrm;
+      if (P.T) P.T[ji] = t_acc * nrm;
+      if (P.V) P.V[ji] = vv;
     }
   }
-  const int a0 = P.sh.ao[a], b0 = P.sh.ao[b];
-#pragma unroll
-  for (int i = 0; i < NA; ++i)
-#pragma unroll
-    for (int j = 0; j < NB; ++j) {
-      const double nrm = cart_norm(LA, i) * cart_norm(LB, j);
-      const int idx = (a0 + i) * P.nao + b0 + j;
-      if (P.S) P.S[idx] = s[i][j] * nrm;
-      if (P.T) P.T[idx] = k[i][j] * nrm;
-      if (P.V) P.V[idx] = v[i][j] * nrm;
-    }
 }
 
-__global__ void one_electron_kernel(OneParams P) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= P.nshell * P.nshell) return;
-  const int a = idx / P.nshell, b = idx % P.nshell;
-  const int la = P.sh.l[a], lb = P.sh.l[b];
-  switch (la * 3 + lb) {
-    case 0: one_pair<0, 0>(P, a, b); break;
-    case 1: one_pair<0, 1>(P, a, b); break;
-    case 2: one_pair<0, 2>(P, a, b); break;
-    case 3: one_pair<1, 0>(P, a, b); break;
-    case 4: one_pair<1, 1>(P, a, b); break;
-    case 5: one_pair<1, 2>(P, a, b); break;
-    case 6: one_pair<2, 0>(P, a, b); break;
-    case 7: one_pair<2, 1>(P, a, b); break;
-    case 8: one_pair<2, 2>(P, a, b); break;
+// one CTA per canonical pair (a >= b): block k = a (a + 1) / 2 + b
+__global__ void __launch_bounds__(kOneThreads) one_electron_kernel(OneParams P) {
+  __shared__ __align__(16) double smem[kOneSmem];
+  const int k = blockIdx.x;
+  int a = (int)((sqrt(8.0 * k + 1.0) - 1.0) * 0.5);
+  while (a * (a + 1) / 2 > k) --a;
+  while ((a + 1) * (a + 2) / 2 <= k) ++a;
+  const int b = k - a * (a + 1) / 2;
+  switch (P.sh.l[a] * 3 + P.sh.l[b]) {
+    case 0: one_pair<0, 0>(P, a, b, smem); break;
+    case 1: one_pair<0, 1>(P, a, b, smem); break;
+    case 2: one_pair<0, 2>(P, a, b, smem); break;
+    case 3: one_pair<1, 0>(P, a, b, smem); break;
+    case 4: one_pair<1, 1>(P, a, b, smem); break;
+    case 5: one_pair<1, 2>(P, a, b, smem); break;
+    case 6: one_pair<2, 0>(P, a, b, smem); break;
+    case 7: one_pair<2, 1>(P, a, b, smem); break;
+    case 8: one_pair<2, 2>(P, a, b, smem); break;
     default: break;
   }
 }
 
 cudaError_t launch_one_electron(const OneParams &P, cudaStream_t st) {
-  const int n = P.nshell * P.nshell;
-  one_electron_kernel<<<(n + 63) / 64, 64, 0, st>>>(P);
+  const int n = P.nshell * (P.nshell + 1) / 2;
+  if (n == 0) return cudaSuccess;
+  one_electron_kernel<<<n, kOneThreads, 0, st>>>(P);
   return cudaGetLastError();
 }
 

@@ -158,11 +158,24 @@ class FockBuilder:
             self.last_stats = st.as_dict()
         return J, K
 
-    def capture_jk(self, D: torch.Tensor, J: torch.Tensor, K: torch.Tensor, precision: str | None = None):
+    def capture_jk(self, D: torch.Tensor, J: torch.Tensor, K: torch.Tensor, precision: str | None = None,
+                   native: bool = False, node_priority: bool = True):
         """Capture one Fock build J, K = jk(D) on these static tensors as a CUDA
         graph (the class launches and their stream fork/join become graph
         nodes); returns the graph -- ``g.replay()`` rebuilds J and K for the
-        current contents of D without any host-side launch work."""
+        current contents of D without any host-side launch work.
+
+        native=False: a torch.cuda.CUDAGraph (composable with torch ops in the
+        same capture).  native=True: the library captures and instantiates the
+        graph itself (sf_fock_jk_graph_create), with node_priority keeping each
+        launch's side-stream priority on replay."""
+        if native:
+            for t in (D, J, K):
+                if t.shape != (self.nao, self.nao) or t.dtype != torch.float64 or t.device != self.device \
+                        or not t.is_contiguous():
+                    raise ValueError("D, J, K must be contiguous (%d,%d) float64 tensors on %s"
+                                     % (self.nao, self.nao, self.device))
+            return _NativeFockGraph(self, D, J, K, _lib.PRECISION[precision or self.precision], node_priority)
         self.jk(D, precision=precision, out=(J, K))          # builds the quartet lists (allocates)
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
@@ -388,3 +401,31 @@ def eri_rys(coefs1, coefs2, coefs3, coefs4, expns1, expns2, expns3, expns4, shel
     finally:
         fb.close()
     return float(blk[comp[0], comp[1], comp[2], comp[3]])
+
+
+class _NativeFockGraph:
+    """A Fock build captured and instantiated by the library (see
+    FockBuilder.capture_jk(native=True)); replay() launches it on the current
+    stream, close() frees it."""
+
+    def __init__(self, fb: "FockBuilder", D, J, K, prec: int, node_priority: bool):
+        self._keep = (fb, D, J, K)
+        self._g = C.c_void_p()
+        with torch.cuda.device(fb.device):
+            _lib.check(_lib.lib().sf_fock_jk_graph_create(fb.handle, _ptr(D), _ptr(J), _ptr(K), prec, fb.cutoff,
+                                                          fb.fp32_cutoff, 1 if node_priority else 0, _stream_ptr(),
+                                                          C.byref(self._g)))
+
+    def replay(self):
+        _lib.check(_lib.lib().sf_fock_graph_launch(self._g, _stream_ptr()))
+
+    def close(self):
+        if self._g:
+            _lib.lib().sf_fock_graph_destroy(self._g)
+            self._g = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -90,6 +90,9 @@ def main(argv=None):
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent grid: CTAs per SM (0: occupancy)")
     ap.add_argument("--density", default="grad", choices=["none", "grad", "fock", "both"],
                     help="density-weighted classification of the quartet lists (sf_set_density_screening)")
+    ap.add_argument("--graph", action="store_true",
+                    help="also time --builds replays of the build captured as a CUDA graph: torch.cuda.CUDAGraph "
+                         "and the library's own capture with and without node priorities")
     ap.add_argument("--grad", action="store_true",
                     help="profile the two-electron gradient (sf_grad_jk) instead of the Fock build")
     ap.add_argument("--one-electron", action="store_true",
@@ -181,6 +184,26 @@ def main(argv=None):
         ev[1].record()
         torch.cuda.synchronize()
         print("wall time of one build (mean of %d back to back): %.4f ms" % (a.builds, ev[0].elapsed_time(ev[1]) / a.builds))
+
+    if a.graph and not a.grad:
+        fb.set_profiling(0)
+        J = torch.empty_like(D)
+        K = torch.empty_like(D)
+        for name, kw in (("torch.cuda.CUDAGraph", {}), ("library graph, node priorities", {"native": True}),
+                         ("library graph, stream priority", {"native": True, "node_priority": False})):
+            g = fb.capture_jk(D, J, K, **kw)
+            for _ in range(3):
+                g.replay()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            for _ in range(a.builds):
+                g.replay()
+            ev[1].record()
+            torch.cuda.synchronize()
+            print("graph replay (%s): %.4f ms per build (mean of %d)" % (name, ev[0].elapsed_time(ev[1]) / a.builds,
+                                                                        a.builds))
+            if hasattr(g, "close"):
+                g.close()
 
 
 if __name__ == "__main__":

@@ -30,3 +30,37 @@ def test_graph_scf_matches_eager(cuda, precision, tol):
     assert r.converged
     assert abs(r.energy - ref.energy) < tol
     assert float((r.D - ref.D).abs().max()) < 1e-4
+
+
+@pytest.mark.parametrize("precision,node_priority", [("fp64", True), ("mixed_df", True), ("mixed_df", False)])
+def test_native_fock_graph_matches_eager(cuda, precision, node_priority):
+    """One Fock build captured and instantiated by the library
+    (sf_fock_jk_graph_create): a replay after D changed gives the eager build
+    of the new D; the persistent launch mode captures the same way."""
+    import torch
+    from segfault_py_gb300 import geometry as G
+    from segfault_py_gb300.fock import FockBuilder
+    from segfault_py_gb300.molecule import Molecule
+    s, x = G.water_cluster(3, seed=4)
+    mol = Molecule.from_geometry(s, x, "6-31g*")
+    fb = FockBuilder(mol, device=cuda, cutoff=1e-12, fp32_cutoff=1e-2)
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((mol.nao, mol.nao)) * 0.1
+    D = torch.tensor(A + A.T, device=cuda)
+    J = torch.empty_like(D)
+    K = torch.empty_like(D)
+    for mode in ("streams", "persistent"):
+        fb.set_launch_mode(mode)
+        g = fb.capture_jk(D, J, K, precision=precision, native=True, node_priority=node_priority)
+        B = rng.standard_normal((mol.nao, mol.nao)) * 0.05
+        D.add_(torch.tensor(B + B.T, device=cuda))
+        g.replay()
+        g.replay()
+        torch.cuda.synchronize()
+        Je, Ke = fb.jk(D, precision=precision)
+        scale = max(float(Je.abs().max()), float(Ke.abs().max()))
+        assert float((J - Je).abs().max()) <= 1e-12 * scale, mode
+        assert float((K - Ke).abs().max()) <= 1e-12 * scale, mode
+        g.close()
+    fb.set_launch_mode("streams")
+    fb.close()
