@@ -212,6 +212,12 @@ typedef struct sf_fock_graph sf_fock_graph;
 int sf_fock_jk_graph_create(sf_handle *h, const double *D, double *J, double *K, int32_t precision, double cutoff,
                             double fp32_cutoff, int32_t node_priority, void *stream, sf_fock_graph **out);
 int sf_fock_graph_launch(sf_fock_graph *g, void *stream);
+/* Instantiate a graph the caller captured and owns (a cudaGraph_t, e.g. the
+ * whole SCF iteration captured by torch.cuda.CUDAGraph(keep_graph=True)),
+ * with node priorities when node_priority != 0, on the current device; launch
+ * and free it with sf_fock_graph_launch / sf_fock_graph_destroy (which leaves
+ * the caller's graph alone).  The graph must outlive the instance. */
+int sf_graph_instantiate(void *graph, int32_t node_priority, sf_fock_graph **out);
 void sf_fock_graph_destroy(sf_fock_graph *g);
 
 /* How a Fock build launches its class kernels (no counterpart in the

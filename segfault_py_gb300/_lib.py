@@ -25,7 +25,7 @@ EXPORTS = ["sf_version", "sf_last_error", "sf_create", "sf_build_shells", "sf_de
            "sf_small_solve", "sf_eri_plan_create", "sf_eri_plan_info", "sf_eri_plan_offsets", "sf_eri_plan_run",
            "sf_eri_plan_destroy", "sf_autotune", "sf_tuning_count", "sf_get_tuning", "sf_set_tuning", "sf_eri_plan_run_md",
            "sf_set_density_screening", "sf_set_launch_mode", "sf_fock_jk_graph_create", "sf_fock_graph_launch",
-           "sf_fock_graph_destroy", "sf_debug_tc_wait_limit", "sf_grad_stats"]
+           "sf_fock_graph_destroy", "sf_debug_tc_wait_limit", "sf_grad_stats", "sf_graph_instantiate"]
 
 
 class SegFockUnavailable(ImportError):
@@ -130,6 +130,7 @@ def lib():
     L.sf_fock_graph_destroy.restype = None
     L.sf_debug_tc_wait_limit.argtypes = [i32]
     L.sf_grad_stats.argtypes = [p, p, p]
+    L.sf_graph_instantiate.argtypes = [p, i32, p]
     _lib = L
     return L
 

@@ -20,7 +20,7 @@ INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(REPO, "_build")
 LIB = os.path.join(CSRC, "libsegfock.so")
 
-CU_SOURCES = ["jk_persist.cu", "jk_dd.cu", "eri_dd.cu", "md_eri.cu", "md_tc.cu", "api.cu", "jk_f64.cu", "jk_f32.cu", "grad_f64.cu", "grad_f32.cu", "grad_dd.cu", "grad_dd_0.cu", "grad_dd_1.cu", "grad_dd_2.cu", "grad_dd_3.cu", "eri.cu", "oneint.cu", "peak.cu", "scf_util.cu"]
+CU_SOURCES = ["jk_persist.cu", "jk_dd.cu", "jk_dd_wide.cu", "eri_dd.cu", "md_eri.cu", "md_tc.cu", "api.cu", "jk_f64.cu", "jk_f32.cu", "grad_f64.cu", "grad_f32.cu", "grad_dd.cu", "grad_dd_0.cu", "grad_dd_1.cu", "grad_dd_2.cu", "grad_dd_3.cu", "eri.cu", "oneint.cu", "peak.cu", "scf_util.cu"]
 CPP_SOURCES = ["rys_table.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

@@ -487,6 +487,11 @@ std::vector<int> lpt_streams(const std::vector<double> &cost_desc, int first = 0
 // number of primitive iterations; inside a cost bucket the (i, j) order of the
 // Schwarz-sorted pair lists is kept.  A partition (part, nparts) keeps every
 // nparts-th quartet of each sorted list, which balances cost across parts.
+// lanes per quartet of a launch of class ci in kind (0 FP64, 1 FP32, 2 dd)
+inline int kind_lanes(const ClassInfo &ci, int kind, int wide) {
+  return kind == 1 ? ci.t32 : (kind == 2 && wide) ? tdd_wide(ci.la, ci.lb, ci.lc, ci.ld, ci.t64) : ci.t64;
+}
+
 int build_work(sf_handle *h, int prec, double cut, double cut32) {
   if (h->c_prec == prec && h->c_cut == cut && h->c_cut32 == cut32 && h->c_part == h->part &&
       h->c_nparts == h->nparts)
@@ -501,6 +506,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     int x0, y0, same;
     int psplit, wsplit;
     int64_t cost_hi;
+    int wide;
   };
   std::vector<Pending> pend;
   h->st_q[0] = h->st_q[1] = h->st_pq[0] = h->st_pq[1] = 0;
@@ -565,6 +571,8 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
         for (int64_t j = lo; j < hi; ++j) lst[pos[(size_t)ka * KB + h->pnp[y0 + j]]++] = make_int2(i, (int)j);
       }
       Pending p;
+      // the double-float accurate tier of a mixed build runs its wide kernels
+      p.wide = (kind == 2 && prec == SF_PREC_MIXED_DF) ? 1 : 0;
       p.cost_hi = 0;
       p.psplit = 1;
       p.wsplit = 1;
@@ -588,7 +596,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       h->st_f[pr] += p.flops;
       // split the cost-sorted list into launches with P primitive sub-groups
       // per quartet: heavy quartets (many primitive quartets) get more lanes
-      const int T = pr == 0 ? ci.t64 : ci.t32;
+      const int T = kind_lanes(ci, kind, p.wide);
       const int pmax = 32 / T;
       auto psplit = [&](int64_t cost) {
         if (pmax > 1 && cost >= 4 * pmax) return pmax;
@@ -648,6 +656,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
     w.psplit = p.psplit;
     w.wsplit = p.wsplit;
     w.max_cost = (int)std::max<int64_t>(p.cost_hi, 1);
+    w.wide = p.wide;
     h->slices.push_back({p.cls, p.prec, w, p.n, p.prims, p.flops, p.cost_hi});
   }
   // greedy longest-processing-time assignment of slices to side streams;
@@ -1461,7 +1470,7 @@ int sf_get_slice_info(sf_handle *h, int32_t idx, sf_slice_info *out) {
     out->prim_quartets = (int64_t)c[1];
     out->flop_alg = (double)c[1] * nr * 4.0 * nabcd + 12.0 * nabcd * (double)c[0];
   }
-  out->threads_per_quartet = (L.kind == 1 ? ci.t32 : ci.t64) * L.w.psplit * L.w.wsplit;
+  out->threads_per_quartet = kind_lanes(ci, L.kind, L.w.wide) * L.w.psplit * L.w.wsplit;
   out->ms = -1.0f;
   out->start_ms = -1.0f;
   out->stream = h->profiling == 2 ? -1 : L.stream;
@@ -1629,6 +1638,22 @@ int sf_fock_jk_graph_create(sf_handle *h, const double *D, double *J, double *K,
   return SF_OK;
 }
 
+int sf_graph_instantiate(void *graph, int32_t node_priority, sf_fock_graph **out) {
+  if (!out) return fail(SF_EINVAL, "sf_graph_instantiate: out is NULL");
+  *out = nullptr;
+  if (!graph) return fail(SF_EINVAL, "sf_graph_instantiate: NULL graph");
+  auto *fg = new sf_fock_graph;
+  SF_CK(cudaGetDevice(&fg->device));
+  const cudaError_t e = cudaGraphInstantiateWithFlags(&fg->exec, (cudaGraph_t)graph,
+                                                      node_priority ? cudaGraphInstantiateFlagUseNodePriority : 0);
+  if (e != cudaSuccess) {
+    delete fg;
+    return fail(SF_ECUDA, std::string("sf_graph_instantiate: ") + cudaGetErrorString(e));
+  }
+  *out = fg;   // fg->graph stays null: the caller owns the graph
+  return SF_OK;
+}
+
 int sf_fock_graph_launch(sf_fock_graph *g, void *stream) {
   if (!g || !g->exec) return fail(SF_EINVAL, "sf_fock_graph_launch: NULL graph");
   DeviceGuard dg(g->device);
@@ -1665,7 +1690,7 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
   // Fock build clears; the caller's matrices are not touched
   auto time_split = [&](const sf_handle::Slice &sl, int S, float *ms) -> cudaError_t {
     const ClassInfo &ci = kClassInfo[sl.cls];
-    const int pmax = 32 / (sl.prec == 1 ? ci.t32 : ci.t64);
+    const int pmax = 32 / kind_lanes(ci, sl.prec, sl.w.wide);
     ClassWork w = sl.w;
     w.psplit = std::min(S, pmax);
     w.wsplit = S / w.psplit;
@@ -1767,7 +1792,7 @@ int sf_autotune(sf_handle *h, const double *D, int32_t precision, double cutoff,
   int tuned = 0;
   for (auto &sl : h->slices) {
     const ClassInfo &ci = kClassInfo[sl.cls];
-    const int pmax = 32 / (sl.prec == 1 ? ci.t32 : ci.t64);
+    const int pmax = 32 / kind_lanes(ci, sl.prec, sl.w.wide);
     const int S0 = sl.w.psplit * sl.w.wsplit;
     float ms0 = 0.f;
     cudaError_t e = time_split(sl, S0, &ms0);

@@ -30,6 +30,18 @@
 
 namespace sf {
 struct ClassInfo { int la, lb, lc, ld, t64, t32; };
+// Lanes per quartet of the double-float kernels run as the accurate tier of a
+// mixed build: twice the FP64 lanes for classes with 18 or more outputs.
+// That tier holds few quartets with long primitive loops (Q_ab Q_cd above
+// the FP32 cutoff) and its launches are latency-bound, so fewer outputs and
+// registers per lane and more warps shorten them ((H2O)8 6-31G* FP32 +
+// double-float build 1.60 -> 1.39 ms); with every quartet in double-float the
+// FP64 lanes stay better ((H2O)16: 24.2 ms against 25.5 ms).
+constexpr int tdd_wide(int la, int lb, int lc, int ld, int t64) {
+  return (la + 1) * (la + 2) / 2 * ((lb + 1) * (lb + 2) / 2) * ((lc + 1) * (lc + 2) / 2) * ((ld + 1) * (ld + 2) / 2) >= 18
+             ? (2 * t64 < 32 ? 2 * t64 : 32)
+             : t64;
+}
 constexpr ClassInfo kClassInfo[21] = {
 #define SF_CI(id, la, lb, lc, ld, t64, t32) {la, lb, lc, ld, t64, t32},
     SF_CLASS_LIST(SF_CI)

@@ -1,5 +1,7 @@
-// jk_dd.cu -- double-float (dd) J/K kernels, one instantiation per class: the accurate tier of the SF_PREC_MIXED_DF / SF_PREC_DF modes.  Lanes
-// per quartet as the FP64 kernels (same register footprint per value).
+// jk_dd.cu -- double-float (dd) J/K kernels, per class: the accurate tier of
+// the SF_PREC_MIXED_DF / SF_PREC_DF modes.  Lanes per quartet as the FP64
+// kernels (same register footprint per value); the tdd_wide instantiations
+// for the accurate tier of a mixed build are in jk_dd_wide.cu.
 #include "classes.h"
 #include "launch.h"
 
@@ -19,8 +21,11 @@ static cudaError_t run_jk_dd(const KParams &kp, const ClassWork &w, const dd *D,
   return cudaGetLastError();
 }
 
+// w.wide selects the tdd_wide lanes per quartet (the accurate tier of a mixed
+// build; compiled in jk_dd_wide.cu), else the FP64 lanes
 cudaError_t launch_jk_dd(int cls, const KParams &kp, const ClassWork &w, const dd *D, double *Jh, double *Kh,
                          cudaStream_t st) {
+  if (w.wide) return launch_jk_dd_wide(cls, kp, w, D, Jh, Kh, st);
   switch (cls) {
 #define SF_CASE(id, la, lb, lc, ld, t64, t32) \
   case id: return run_jk_dd<la, lb, lc, ld, t64>(kp, w, D, Jh, Kh, st);
@@ -36,6 +41,7 @@ cudaError_t prepare_jk_dd() {
   if (e == cudaSuccess) e = prep_smem(jk_kernel<la, lb, lc, ld, dd, t64>, grp_smem<la, lb, lc, ld, dd, t64>());
   SF_CLASS_LIST(SF_PREP)
 #undef SF_PREP
+  if (e == cudaSuccess) e = prepare_jk_dd_wide();
   return e;
 }
 

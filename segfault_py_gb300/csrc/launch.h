@@ -10,6 +10,10 @@ cudaError_t launch_jk_f32(int cls, const KParams &kp, const ClassWork &w, const 
                           cudaStream_t st);
 cudaError_t launch_jk_dd(int cls, const KParams &kp, const ClassWork &w, const dd *D, double *Jh, double *Kh,
                          cudaStream_t st);
+// the same with tdd_wide lanes per quartet (jk_dd_wide.cu)
+cudaError_t launch_jk_dd_wide(int cls, const KParams &kp, const ClassWork &w, const dd *D, double *Jh, double *Kh,
+                              cudaStream_t st);
+cudaError_t prepare_jk_dd_wide();
 // persistent multi-class FP32 J/K kernels (jk_persist.cu): one launch per
 // register tier runs the tiles of every list of the tier's classes, taken
 // from a device work queue

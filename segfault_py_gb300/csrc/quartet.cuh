@@ -1102,6 +1102,7 @@ struct ClassWork {
   // device count of the quartets actually in the list (lists compacted on the
   // device by the density-weighted classification); nullptr: n
   const unsigned long long *count = nullptr;
+  int wide = 0;            // double-float: the tdd_wide lanes per quartet (host-side choice)
 };
 
 // quartets of a work list: the device count when the list was compacted on

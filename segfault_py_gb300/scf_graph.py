@@ -21,7 +21,10 @@ whole iteration replays as a single graph launch:
 * Fock build: FockBuilder.jk into static buffers (the library launches its
   class kernels on streams forked from the capturing stream).
 The host replays the graph once per iteration and reads dE from pinned
-memory; convergence is checked exactly as in the reference.
+memory; convergence is checked exactly as in the reference.  Where torch
+keeps the captured graph (CUDAGraph(keep_graph=True)) the library
+instantiates it with node priorities (sf_graph_instantiate), so the Fock
+build's accurate tier keeps its high-priority side streams on replay.
 """
 from __future__ import annotations
 
@@ -79,6 +82,7 @@ class GraphSCF:
         self.slots = torch.arange(NSLOT, dtype=torch.float64, device=dev)
         self.dE_host = torch.zeros((), dtype=torch.float64).pin_memory()
         self.graph = None
+        self._exec = None
 
     # ------------------------------------------------------------------
     def _purify(self, Fp):
@@ -135,6 +139,9 @@ class GraphSCF:
     # ------------------------------------------------------------------
     def capture(self):
         """Warm up (builds the quartet lists, cuBLAS handles) and capture."""
+        if self._exec is not None:
+            _lib.lib().sf_fock_graph_destroy(self._exec)
+            self._exec = None
         state = [t.clone() for t in (self.F, self.Eold, self.count, self.Fs, self.Rs, self.mask, self.slot)]
         s = torch.cuda.Stream(device=self.dev)
         s.wait_stream(torch.cuda.current_stream())
@@ -145,11 +152,41 @@ class GraphSCF:
         for t, v in zip((self.F, self.Eold, self.count, self.Fs, self.Rs, self.mask, self.slot), state):
             t.copy_(v)
         torch.cuda.synchronize()
-        self.graph = torch.cuda.CUDAGraph()
+        # keep the captured cudaGraph_t where torch allows it and instantiate it
+        # through the library with node priorities: replayed by torch, every
+        # node runs at the launching stream's priority and the Fock build's
+        # accurate tier loses the high-priority side streams it has eagerly
+        try:
+            self.graph = torch.cuda.CUDAGraph(keep_graph=True)
+            keep = True
+        except TypeError:
+            self.graph = torch.cuda.CUDAGraph()
+            keep = False
         with torch.cuda.graph(self.graph):
             self._iteration()
         torch.cuda.synchronize()
+        self._exec = None
+        if keep:
+            h = C.c_void_p()
+            _lib.check(_lib.lib().sf_graph_instantiate(C.c_void_p(int(self.graph.raw_cuda_graph())), 1, C.byref(h)))
+            self._exec = h
         return self
+
+    def _replay(self):
+        if self._exec is not None:
+            _lib.check(_lib.lib().sf_fock_graph_launch(self._exec,
+                                                       C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        else:
+            self.graph.replay()
+
+    def __del__(self):
+        ex = getattr(self, "_exec", None)
+        if ex is not None:
+            try:
+                _lib.lib().sf_fock_graph_destroy(ex)
+            except Exception:
+                pass
+            self._exec = None
 
     def run(self, tol: float = 1e-8, maxiter: int = 100) -> SCFResult:
         if self.graph is None:
@@ -158,7 +195,7 @@ class GraphSCF:
         it = 0
         hist = []
         while True:
-            self.graph.replay()
+            self._replay()
             self.dE_host.copy_(self.dE, non_blocking=True)
             torch.cuda.current_stream().synchronize()
             hist.append(float(self.E) + self.mol.e_nuc)
@@ -174,7 +211,7 @@ class GraphSCF:
                          H=self.H, S=self.S, history=hist)
 
     def replay_once(self):
-        self.graph.replay()
+        self._replay()
 
 
 def scf_graph(mol: Molecule, tol=1e-8, maxiter=100, precision="fp64", cutoff=1e-12, fp32_cutoff=1e-2, fb=None,
