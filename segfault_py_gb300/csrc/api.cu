@@ -17,6 +17,8 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <thread>
+#include <atomic>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -513,15 +515,24 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
   h->st_f[0] = h->st_f[1] = 0.0;
   h->st_total = 0;
   constexpr int KB = kMaxPrim * kMaxPrim + 1;   // primitive pairs per shell pair <= 256
-  std::vector<int64_t> hist((size_t)KB * KB);
-  for (int cls = 0; cls < kNumClass; ++cls) {
+  // every class's lists are cut independently, on host threads, then
+  // concatenated in class order (the result does not depend on the threads)
+  struct Part {   // the list of one (class, tier), offsets relative to it
+    std::vector<int2> lst;
+    std::vector<Pending> segs;
+    int64_t q = 0, pq = 0;
+    double f = 0.0;
+  };
+  std::vector<Part> parts(2 * kNumClass);
+  std::vector<int64_t> totals(kNumClass, 0);
+  auto build_class = [&](int cls, std::vector<int64_t> &hist) {
     const ClassInfo &ci = kClassInfo[cls];
     const int X = pair_class_of(ci.la, ci.lb), Y = pair_class_of(ci.lc, ci.ld);
     const int x0 = h->cstart[X], y0 = h->cstart[Y];
     const int nX = h->cstart[X + 1] - x0, nY = h->cstart[Y + 1] - y0;
     const int same = X == Y;
-    h->st_total += same ? (int64_t)nX * (nX + 1) / 2 : (int64_t)nX * nY;
-    if (nX == 0 || nY == 0) continue;
+    totals[cls] = same ? (int64_t)nX * (nX + 1) / 2 : (int64_t)nX * nY;
+    if (nX == 0 || nY == 0) return;
     const double *qx = h->pq.data() + x0, *qy = h->pq.data() + y0;
     std::vector<int64_t> m(nX), m64(nX);
     for (int i = 0; i < nX; ++i) {
@@ -578,7 +589,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       p.wsplit = 1;
       p.cls = cls;
       p.prec = kind;
-      p.off = all.size();
+      p.off = 0;
       p.x0 = x0;
       p.y0 = y0;
       p.same = same;
@@ -591,9 +602,10 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
       p.n = (int64_t)lst.size();
       p.prims = (int64_t)(prims * frac);
       p.flops = ((double)prims * nr * 4.0 * nabcd + 12.0 * nabcd * (double)n) * frac;
-      h->st_q[pr] += p.n;
-      h->st_pq[pr] += p.prims;
-      h->st_f[pr] += p.flops;
+      Part &part = parts[2 * cls + pr];
+      part.q = p.n;
+      part.pq = p.prims;
+      part.f = p.flops;
       // split the cost-sorted list into launches with P primitive sub-groups
       // per quartet: heavy quartets (many primitive quartets) get more lanes
       const int T = kind_lanes(ci, kind, p.wide);
@@ -627,7 +639,7 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
         int64_t q1 = q0 + 1;
         while (q1 < p.n && split_of(cost_of(q1)) == S) ++q1;
         Pending seg = p;
-        seg.off = all.size() + q0;
+        seg.off = q0;
         seg.n = q1 - q0;
         seg.cost_hi = cost_of(q0);
         int St = S;
@@ -639,10 +651,37 @@ int build_work(sf_handle *h, int prec, double cut, double cut32) {
         for (int64_t q = q0; q < q1; ++q) sp += cost_of(q);
         seg.prims = sp;
         seg.flops = (double)sp * nr * 4.0 * nabcd + 12.0 * nabcd * (double)seg.n;
-        pend.push_back(seg);
+        part.segs.push_back(seg);
         q0 = q1;
       }
-      all.insert(all.end(), lst.begin(), lst.end());
+      part.lst = std::move(lst);
+    }
+    };
+  {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nthr = std::max(1, std::min<int>(kNumClass, hw ? (int)hw : 1));
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+      std::vector<int64_t> hist((size_t)KB * KB);
+      for (int c = next++; c < kNumClass; c = next++) build_class(c, hist);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthr; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+  }
+  for (int cls = 0; cls < kNumClass; ++cls) {
+    h->st_total += totals[cls];
+    for (int pr = 0; pr < 2; ++pr) {
+      Part &part = parts[2 * cls + pr];
+      for (Pending seg : part.segs) {
+        seg.off += all.size();
+        pend.push_back(seg);
+      }
+      all.insert(all.end(), part.lst.begin(), part.lst.end());
+      h->st_q[pr] += part.q;
+      h->st_pq[pr] += part.pq;
+      h->st_f[pr] += part.f;
     }
   }
   SF_CK(h->d_list.upload(all));
