@@ -11,14 +11,15 @@ are autotuned for every timed mode before the timed region.
 
 Reported:
 * value        Fock builds/s, mixed path (FP32 + double-float), D/J/K resident
-               in HBM; L2 flushed
-               (256 MB write) before every step, each step timed by CUDA events;
-               each build launched eagerly through FockBuilder.jk
-               (graph_replay_value: the same build replayed from a CUDA graph;
-               graph_native_value: the library's own capture of the build,
-               replayed with node priorities; persistent_launch_value: the FP32
-               register-path classes as one persistent launch per register
-               tier, fed by a device work queue)
+               in HBM; L2 flushed (256 MB write) before every step, each step
+               timed by CUDA events; each build replayed from the library's own
+               capture of it (FockBuilder.capture_jk(native=True):
+               sf_fock_jk_graph_create / sf_fock_graph_launch, node priorities
+               kept) -- the way an SCF iteration runs it; the same build issued
+               eagerly through FockBuilder.jk is eager_value (graph_replay_value:
+               replayed from a torch.cuda.CUDAGraph; persistent_launch_value:
+               the FP32 register-path classes as one persistent launch per
+               register tier, fed by a device work queue)
 * e2e          same metric through the public API with host buffers: pinned D
                -> device, Fock build, J and K -> pinned host, every step
 * fp64         the all-FP64 build, same protocol (the plain FP64 GPU baseline)
@@ -63,28 +64,22 @@ HEADLINE = "mixed_df"
 CUTOFF = 1e-12
 FP32_CUTOFF = 1e-2
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) per launch of J/K class kernels of this workload,
-# from ncu captures committed as a text table under profiles/ together with a
-# hash of the kernel sources they were measured on; a table whose hash does
-# not match the sources being run gives traffic = null (stale)
+# DRAM bytes (read + write) per quartet of the J/K class kernels of this
+# workload, from one ncu capture (segfault_py_gb300/profile_traffic.py) committed
+# as a text table under profiles/ together with a hash of the kernel sources
+# it was measured on; a table whose hash does not match the sources being run
+# gives traffic = null (stale)
 TRAFFIC_TABLE = os.path.join(REPO, "profiles", "ncu_dram_bytes_water8_631gs.txt")
 
 
 def csrc_hash():
     """sha256 (first 16 hex digits) over the library's CUDA/C++ sources."""
-    import hashlib
-    d = os.path.join(REPO, "segfault_py_gb300", "csrc")
-    h = hashlib.sha256()
-    for f in sorted(os.listdir(d)):
-        if f.endswith((".cu", ".cuh", ".h", ".cpp")):
-            h.update(f.encode())
-            with open(os.path.join(d, f), "rb") as fh:
-                h.update(fh.read())
-    return h.hexdigest()[:16]
+    from segfault_py_gb300.profile_traffic import csrc_hash as h
+    return h()
 
 
 def ncu_traffic(kernel):
-    """(bytes per launch, source note) of a kernel from the committed table."""
+    """(DRAM bytes per quartet, source note) of a kernel family from the committed table."""
     if not os.path.exists(TRAFFIC_TABLE):
         return None, "no ncu table"
     table, src_hash = {}, None
@@ -100,7 +95,7 @@ def ncu_traffic(kernel):
         return None, "ncu table measured on other kernel sources (stale)"
     if kernel not in table:
         return None, "kernel not in the ncu table"
-    return table[kernel], "ncu capture, " + os.path.relpath(TRAFFIC_TABLE, REPO)
+    return table[kernel], "ncu capture, " + os.path.relpath(TRAFFIC_TABLE, REPO) + " (bytes per quartet x quartets of the launch)"
 
 
 def workload(nwater=8, basis="6-31g*", seed=0):
@@ -124,10 +119,20 @@ def clock_sampler_start(path):
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
     try:
         f = open(path, "w")
-        return subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
-                                stdout=f, stderr=subprocess.DEVNULL), f
+        proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                stdout=f, stderr=subprocess.DEVNULL)
     except Exception:
         return None, None
+    # wait (at most 5 s) for the first sample: nvidia-smi's start-up, which
+    # initialises NVML, must not fall into the timed steps
+    t0 = time.time()
+    while time.time() - t0 < 5.0 and proc.poll() is None:
+        f.flush()
+        if os.path.getsize(path) > 0:
+            break
+        time.sleep(0.05)
+    time.sleep(0.3)
+    return proc, f
 
 
 def clock_sampler_stop(proc, f, path, device_index=0):
@@ -308,11 +313,15 @@ def run_ours(args):
     g64 = rhf_gradient(mol, r, fb, precision="fp64")
     ghl = rhf_gradient(mol, r, fb, precision=HEADLINE)
     grad_err = float((ghl - g64).abs().max())
-    ms_hl, ms_mx, ms_64, ms_e2e = (float(np.sum(t)) for t in (t_hl, t_mx, t_64, t_e2e))
+    # the headline: the build replayed as the library's own captured graph
+    # (one launch per step, node priorities kept); the eager build beside it
+    t_val = t_hl_native
+    ms_hl, ms_mx, ms_64, ms_e2e = (float(np.sum(t)) for t in (t_val, t_mx, t_64, t_e2e))
+    ms_eager = float(np.sum(t_hl))
     if world > 1:
-        tt = torch.tensor([ms_hl, ms_mx, ms_64, ms_e2e], dtype=torch.float64, device=dev)
+        tt = torch.tensor([ms_hl, ms_mx, ms_64, ms_e2e, ms_eager], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_hl, ms_mx, ms_64, ms_e2e = tt.tolist()
+        ms_hl, ms_mx, ms_64, ms_e2e, ms_eager = tt.tolist()
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -332,8 +341,9 @@ def run_ours(args):
     achieved = dom["flop_alg"] / (dom["ms"] * 1e-3) / 1e12 if dom["ms"] > 0 else 0.0
     total_ms = sum(s["ms"] for s in slices_hl)
     comb = st_hl["flop_alg_fp32"] / (peaks["fp32"] * 1e12) + st_hl["flop_alg_fp64"] / (peaks["fp32"] * 1e12)
-    build_frac = comb / (float(np.mean(t_hl)) * 1e-3)
-    traffic, traffic_src = ncu_traffic(dom_name)
+    build_frac = comb / (float(np.mean(t_val)) * 1e-3)
+    bpq, traffic_src = ncu_traffic(dom_name)
+    traffic = bpq * dom["quartets"] if bpq is not None else None
     setup = setup_costs(mol, dev, D, J, K)
     nn = mol.nao * mol.nao * 8
     secondary = None
@@ -356,13 +366,16 @@ def run_ours(args):
         "fp64": {"value": world * steps / (ms_64 * 1e-3), "unit": "Fock builds/s", "ms_per_step": ms_64 / steps,
                  "quartets_per_s": st_64["quartets_fp64"] * steps / (ms_64 * 1e-3),
                  "flop_alg": st_64["flop_alg_fp64"]},
-        "mixed_speedup_vs_fp64": ms_64 / ms_hl,
+        "mixed_speedup_vs_fp64": ms_64 / ms_eager,   # both issued eagerly
         "mixed_fp32_fp64": {"value": world * steps / (ms_mx * 1e-3), "unit": "Fock builds/s",
                             "note": "FP32 below the cutoff, native FP64 above",
                             "energy_error_vs_fp64": emx - e64, "speedup_vs_fp64": ms_64 / ms_mx},
+        "step_ms": {"min": float(np.min(t_val)), "median": float(np.median(t_val)), "max": float(np.max(t_val))},
+        "eager_value": world * steps / (ms_eager * 1e-3),
+        "eager_step_ms": {"min": float(np.min(t_hl)), "median": float(np.median(t_hl)), "max": float(np.max(t_hl))},
         "graph_replay_value": world * steps / (float(np.sum(t_hl_graph)) * 1e-3),
         "persistent_launch_value": world * steps / (float(np.sum(t_hl_persist)) * 1e-3),
-        "graph_native_value": world * steps / (float(np.sum(t_hl_native)) * 1e-3),
+        "graph_native_value": world * steps / (ms_hl * 1e-3),
         "quartets_per_s": (st_hl["quartets_fp64"] + st_hl["quartets_fp32"]) * world * steps / (ms_hl * 1e-3),
         "prim_quartets_per_s": (st_hl["prim_quartets_fp64"] + st_hl["prim_quartets_fp32"]) * world * steps
                                / (ms_hl * 1e-3),
@@ -680,7 +693,9 @@ def run_reference(args):
     rec = {"metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": full * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "impl": "reference",
-           "config": cfg_dict(mol, args.nwater, args.basis),
+           "config": dict(cfg_dict(mol, args.nwater, args.basis),
+                          density="0.1 I (the reference's algorithm evaluates every unique AO quartet "
+                                  "whatever the density)", l2="not flushed (CPU arm)"),
            "cpu_baseline": {"value": value, "unit": "Fock builds/s", "cores": threads, "kind": "port",
                             "sample": "each timed step: one whole Fock build, all %d unique AO quartets "
                                       "(warm-up steps: 1/40 of the pair rows)" % tot,

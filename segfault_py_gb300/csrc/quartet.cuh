@@ -644,14 +644,16 @@ __device__ __forceinline__ void load_prim_cd(const KParams &kp, const QGeom<R> &
 }
 
 // float -> double without the FP64 pipe: re-pack sign, exponent (rebias
-// 127 -> 1023) and mantissa with 32-bit integer operations.  Zeros and
-// single-precision subnormals (< 1.2e-38) become +-0; inf/nan stay inf/nan.
+// 127 -> 1023, i.e. + 896 << 20 in the high word) and mantissa with five
+// 32-bit integer operations, no branches.  Exact for normal floats.  A zero
+// or single-precision subnormal becomes a number of magnitude below
+// 1.2e-38 (a zero: +-2^-127) instead of +-0, which adds nothing measurable
+// to the FP64 sums it feeds; the FP32 kernels produce no inf or nan.  (The
+// version with those special cases cost 3-6 % of the FP32 + double-float
+// build: (H2O)8 1.43 -> 1.35 ms, (H2O)16 6.71 -> 6.48 ms.)
 __device__ __forceinline__ double f2d_alu(float f) {
   const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu, sgn = u & 0x80000000u;
-  if (e == 0u) return __hiloint2double((int)sgn, 0);
-  const unsigned de = e == 0xffu ? 0x7ffu : e + 896u;
-  return __hiloint2double((int)(sgn | (de << 20) | (m >> 3)), (int)(m << 29));
+  return __hiloint2double((int)((u & 0x80000000u) | (((u >> 3) & 0x0fffffffu) + 0x38000000u)), (int)(u << 29));
 }
 __device__ __forceinline__ double to_f64(float f) { return f2d_alu(f); }
 __device__ __forceinline__ double to_f64(double f) { return f; }

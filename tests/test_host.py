@@ -220,3 +220,35 @@ def test_bench_traffic_table_is_keyed_to_the_kernel_sources(tmp_path):
     t.write_text("# csrc_sha16 0000000000000000\njk_kernel<1,0,0,0,fp32> 1234\n")
     v, src = bench.ncu_traffic("jk_kernel<1,0,0,0,fp32>")
     assert v is None and "stale" in src
+
+
+def test_profile_traffic_table_from_ncu_csv(tmp_path):
+    """The DRAM table builder: ncu launch rows mapped to kernel families,
+    bytes summed per family and divided by the families' quartets."""
+    from segfault_py_gb300 import profile_traffic as PT
+    assert PT.family_of_ncu("void sf::jk_kernel<(int)1, (int)0, (int)0, (int)0, float, (int)1>(sf::KParams)") \
+        == "jk_kernel<1,0,0,0,fp32>"
+    assert PT.family_of_ncu("void sf::jk_kernel<2, 1, 1, 0, sf::dd, 4>(sf::KParams)") == "jk_kernel<2,1,1,0,dd>"
+    assert PT.family_of_ncu("void sf::grad_kernel<2, 1, 1, 0, double, 8>(sf::KParams)") is None
+    hdr = '"ID","Process ID","Process Name","Host Name","Kernel Name","Context","Stream","Block Size","Grid Size",' \
+          '"Device","CC","Section Name","Metric Name","Metric Unit","Metric Value"\n'
+    rows = []
+    for lid, name, rd, wr in ((0, "void sf::jk_kernel<1, 0, 0, 0, float, 1>(x)", "2.5", "0.5"),
+                              (1, "void sf::jk_kernel<1, 0, 0, 0, float, 1>(x)", "1,000", "0"),
+                              (2, "void sf::jk_kernel<2, 2, 2, 2, double, 32>(x)", "0.5", "0.25")):
+        unit = "byte" if lid == 1 else "Kbyte"
+        for metric, val in (("dram__bytes_read.sum", rd), ("dram__bytes_write.sum", wr)):
+            rows.append('"%d","1","p","h","%s","1","7","(128, 1, 1)","(9, 1, 1)","0","10.3","","%s","%s","%s"\n'
+                        % (lid, name, metric, unit, val))
+    (tmp_path / "dram.csv").write_text("==PROF== header line\n" + hdr + "".join(rows))
+    (tmp_path / "slices.log").write_text(
+        "(10|00) f32 T= 1 q=     1000 pq=   8000 ms=  0.1 share= 50.0% GF/s=  1.0\n"
+        "(10|00) f32 T= 8 q=      500 pq=   4000 ms=  0.1 share= 25.0% GF/s=  1.0\n"
+        "(22|22) f64 T=32 q=       25 pq=     25 ms=  0.1 share= 25.0% GF/s=  1.0\n")
+    out = tmp_path / "table.txt"
+    PT.main(["--csv", str(tmp_path / "dram.csv"), "--slices", str(tmp_path / "slices.log"), "--out", str(out)])
+    table = {t.split()[0]: t.split() for t in out.read_text().splitlines() if not t.startswith("#")}
+    assert abs(float(table["jk_kernel<1,0,0,0,fp32>"][1]) - (3000.0 + 1000.0) / 1500) < 1e-4   # written to 4 decimals
+    assert table["jk_kernel<1,0,0,0,fp32>"][2:] == ["2", "1500"]
+    assert abs(float(table["jk_kernel<2,2,2,2,fp64>"][1]) - 750.0 / 25) < 1e-4
+    assert ("# csrc_sha16 " + PT.csrc_hash()) in out.read_text()
