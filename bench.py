@@ -365,7 +365,10 @@ def run_ours(args):
                 "h2d_bytes_per_step": nn, "d2h_bytes_per_step": 2 * nn},
         "fp64": {"value": world * steps / (ms_64 * 1e-3), "unit": "Fock builds/s", "ms_per_step": ms_64 / steps,
                  "quartets_per_s": st_64["quartets_fp64"] * steps / (ms_64 * 1e-3),
-                 "flop_alg": st_64["flop_alg_fp64"]},
+                 "flop_alg": st_64["flop_alg_fp64"],
+                 # algorithmic FLOPs per build over its time against the FP64 FMA peak (a lower
+                 # bound: ncu puts the FP64 pipe of its largest kernels at 88-89 % busy)
+                 "frac_of_fp64_peak": st_64["flop_alg_fp64"] / (ms_64 / steps * 1e-3) / (peaks["fp64"] * 1e12)},
         "mixed_speedup_vs_fp64": ms_64 / ms_eager,   # both issued eagerly
         "mixed_fp32_fp64": {"value": world * steps / (ms_mx * 1e-3), "unit": "Fock builds/s",
                             "note": "FP32 below the cutoff, native FP64 above",
