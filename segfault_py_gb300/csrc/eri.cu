@@ -1,4 +1,5 @@
 // eri.cu -- raw contracted ERIs (FP64 / FP32) and Schwarz bounds (FP64).
+#include <algorithm>
 #include "classes.h"
 #include "launch.h"
 
@@ -12,8 +13,12 @@ static cudaError_t run_eri(const KParams &kp, const EriWork &w, cudaStream_t st)
   EriWork w2 = w;
   w2.psplit = P;
   const int G = kBlock / (T * P);
-  constexpr size_t smem = grp_smem<LA, LB, LC, LD, R, T>();
-  const int64_t grid = (w.n + G - 1) / G;
+  size_t smem = grp_smem<LA, LB, LC, LD, R, T>();
+  int64_t grid = (w.n + G - 1) / G;
+  if (T == 1 && std::is_same<R, float>::value) {   // Rys table block in shared memory, grid-stride
+    smem = (size_t)kTabNint * QC<LA, LB, LC, LD>::NR * kTab32Row * sizeof(float);
+    grid = std::min<int64_t>(grid, (int64_t)std::max(kp.nsm, 1) * 16);
+  }
   eri_kernel<LA, LB, LC, LD, R, T><<<(unsigned)grid, kBlock, smem, st>>>(kp, w2);
   return cudaGetLastError();
 }

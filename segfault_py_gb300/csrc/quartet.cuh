@@ -1217,29 +1217,53 @@ struct EriWork {
   int psplit;                  // P primitive sub-groups per quartet (T*P <= 32)
 };
 
+// one quartet of the one-lane (T == 1) raw-integral path: P lanes share it
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void eri_t1_quartet(const KParams &kp, const EriWork &w, int64_t q, int p, int P,
+                                               unsigned qmask, const float *tab_s) {
+  using Q = QC<LA, LB, LC, LD>;
+  const int fl = w.flags[q];
+  const QGeom<R> g = make_geom<R>(kp, w.pab[q], w.pcd[q], fl & 1, fl & 2);
+  R acc[Q::NABCD];
+  eval_t1<LA, LB, LC, LD, R>(kp, g, acc, p, P, tab_s);
+  if (P > 1) reduce_psplit<R, Q::NABCD, 1>(acc, P, qmask);
+  if (p != 0) return;
+  const int s0 = w.strides[4 * q], s1 = w.strides[4 * q + 1], s2 = w.strides[4 * q + 2], s3 = w.strides[4 * q + 3];
+  double *out = w.out + w.out_off[q];
+#pragma unroll
+  for (int o = 0; o < Q::NABCD; ++o)
+    out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = to_f64(acc[o] * (R)Q::norm(o));
+}
+
 template <int LA, int LB, int LC, int LD, typename R, int T>
 __global__ void __launch_bounds__(kBlock) eri_kernel(KParams kp, EriWork w) {
   using Q = QC<LA, LB, LC, LD>;
   const int P = w.psplit;
   const int TP = T * P;
   const int grp = threadIdx.x / TP, p = (threadIdx.x / T) % P, t = threadIdx.x % T;
-  const int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp;
-  if (q >= w.n) return;
-  const int fl = w.flags[q];
-  const QGeom<R> g = make_geom<R>(kp, w.pab[q], w.pcd[q], fl & 1, fl & 2);
-  const int s0 = w.strides[4 * q], s1 = w.strides[4 * q + 1], s2 = w.strides[4 * q + 2], s3 = w.strides[4 * q + 3];
-  double *out = w.out + w.out_off[q];
   const int lane = threadIdx.x & 31;
   const unsigned qmask = (TP == 32) ? 0xffffffffu : (((1u << TP) - 1u) << (lane & ~(TP - 1)));
   if constexpr (T == 1) {
-    R acc[Q::NABCD];
-    eval_t1<LA, LB, LC, LD, R>(kp, g, acc, p, P);
-    if (P > 1) reduce_psplit<R, Q::NABCD, 1>(acc, P, qmask);
-    if (p != 0) return;
-#pragma unroll
-    for (int o = 0; o < Q::NABCD; ++o)
-      out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = to_f64(acc[o] * (R)Q::norm(o));
+    // one lane group per quartet, grid-stride over the list; the FP32 path
+    // copies the n-root block of the Rys table to shared memory once per CTA
+    // (its rows are read at lane-dependent intervals)
+    const float *tab_s = nullptr;
+    if constexpr (std::is_same<R, float>::value) {
+      extern __shared__ __align__(16) unsigned char smem_t[];
+      load_tab32_block(kp, Q::NR, reinterpret_cast<float4 *>(smem_t));
+      __syncthreads();
+      tab_s = reinterpret_cast<const float *>(smem_t);
+    }
+    const int64_t stride = (int64_t)gridDim.x * (kBlock / TP);
+    for (int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp; q < w.n; q += stride)
+      eri_t1_quartet<LA, LB, LC, LD, R>(kp, w, q, p, P, qmask, tab_s);
   } else {
+    const int64_t q = (int64_t)blockIdx.x * (kBlock / TP) + grp;
+    if (q >= w.n) return;
+    const int fl = w.flags[q];
+    const QGeom<R> g = make_geom<R>(kp, w.pab[q], w.pcd[q], fl & 1, fl & 2);
+    const int s0 = w.strides[4 * q], s1 = w.strides[4 * q + 1], s2 = w.strides[4 * q + 2], s3 = w.strides[4 * q + 3];
+    double *out = w.out + w.out_off[q];
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using GP = Grp<LA, LB, LC, LD, R, T>;
     R *buf = reinterpret_cast<R *>(smem_raw) + (threadIdx.x / T) * GP::BUFN;
