@@ -839,7 +839,21 @@ __device__ __forceinline__ void eval_t1(const KParams &kp, const QGeom<R> &g, R 
 template <int LA, int LB, int LC, int LD, typename R, int T>
 struct Grp {
   using Q = QC<LA, LB, LC, LD>;
-  static constexpr int NPER = (Q::NABCD + T - 1) / T;
+  // Outputs per lane.  FP32 groups own whole rows: the INNER outputs that
+  // differ only in the components of the last shell with l > 0 (d, or c when
+  // l_d = 0).  A row's 2-D factors in each direction are the LI+1 consecutive
+  // table entries of that shell's exponents, loaded once per root and shared
+  // by its INNER outputs (3 (LI+1) shared loads per root instead of 3 INNER:
+  // the FP32 contraction is bound by shared-memory loads, FP64 by its pipe).
+  // Otherwise output o = t + k T.
+  static constexpr bool ROWWISE = std::is_same<R, float>::value && (LD > 0 || LC > 0);
+  static constexpr int LI = LD > 0 ? LD : LC;
+  static constexpr int INNER = ROWWISE ? (LD > 0 ? Q::ND : Q::NC) : 1;
+  static constexpr int ROWS = Q::NABCD / INNER;
+  static constexpr int RPER = (ROWS + T - 1) / T;
+  static constexpr int NPER = RPER * INNER;
+  // output of lane t's k-th accumulator (>= NABCD past the last row)
+  __device__ static __forceinline__ int out(int t, int k) { return (t + (k / INNER) * T) * INNER + k % INNER; }
   static constexpr int TABN = 3 * Q::NR * Q::SZ;            // 2-D tables of one primitive quartet
   static constexpr int ROOTS = TABN;                         // then u_r, w_r
   static constexpr int NEED = (TABN + 2 * Q::NR) > Q::NABCD ? (TABN + 2 * Q::NR) : Q::NABCD;
@@ -853,14 +867,19 @@ __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R
                                          R (&acc)[Grp<LA, LB, LC, LD, R, T>::NPER], int p = 0, int P = 1) {
   using Q = QC<LA, LB, LC, LD>;
   using GP = Grp<LA, LB, LC, LD, R, T>;
-  constexpr int NR = Q::NR, SZ = Q::SZ, NPER = GP::NPER;
-  int off[NPER];
+  constexpr int NR = Q::NR, SZ = Q::SZ, NPER = GP::NPER, RPER = GP::RPER, INNER = GP::INNER, LI = GP::LI;
 #pragma unroll
-  for (int k = 0; k < NPER; ++k) {
-    const int o = t + k * T;
-    acc[k] = (R)0;
-    off[k] = o < Q::NABCD ? (Q::toff(o, 0) | ((NR * SZ + Q::toff(o, 1)) << 10) |
-                             ((2 * NR * SZ + Q::toff(o, 2)) << 20))
+  for (int k = 0; k < NPER; ++k) acc[k] = (R)0;
+  // per row: the table offsets of its first output in the three directions,
+  // less the inner shell's exponent of component 0 (the row's base)
+  int off[RPER];
+#pragma unroll
+  for (int j = 0; j < RPER; ++j) {
+    const int o = (t + j * T) * INNER;
+    const int i0 = INNER > 1 ? cart_e(LI, 0, 0) : 0, i1 = INNER > 1 ? cart_e(LI, 0, 1) : 0,
+              i2 = INNER > 1 ? cart_e(LI, 0, 2) : 0;
+    off[j] = o < Q::NABCD ? ((Q::toff(o, 0) - i0) | ((NR * SZ + Q::toff(o, 1) - i1) << 10) |
+                             ((2 * NR * SZ + Q::toff(o, 2) - i2) << 20))
                           : 0;
   }
   const int nprim = g.ab_n * g.cd_n;
@@ -907,13 +926,34 @@ __device__ __forceinline__ void eval_grp(const KParams &kp, const QGeom<R> &g, R
     }
     __syncwarp(gmask);
 #pragma unroll
-    for (int k = 0; k < NPER; ++k) {
-      if (t + k * T < Q::NABCD) {
-        const int ox = off[k] & 1023, oy = (off[k] >> 10) & 1023, oz = off[k] >> 20;
-        R v = (R)0;
+    for (int j = 0; j < RPER; ++j) {
+      if (t + j * T < GP::ROWS) {
+        const int ox = off[j] & 1023, oy = (off[j] >> 10) & 1023, oz = off[j] >> 20;
+        if constexpr (INNER == 1) {
+          R v = (R)0;
 #pragma unroll
-        for (int r = 0; r < NR; ++r) v += tab[ox + r * SZ] * tab[oy + r * SZ] * tab[oz + r * SZ];
-        acc[k] += v;
+          for (int r = 0; r < NR; ++r) v += tab[ox + r * SZ] * tab[oy + r * SZ] * tab[oz + r * SZ];
+          acc[j] += v;
+        } else {
+          R v[INNER];
+#pragma unroll
+          for (int e = 0; e < INNER; ++e) v[e] = (R)0;
+#pragma unroll
+          for (int r = 0; r < NR; ++r) {
+            R X[LI + 1], Y[LI + 1], Z[LI + 1];
+#pragma unroll
+            for (int i = 0; i <= LI; ++i) {
+              X[i] = tab[ox + r * SZ + i];
+              Y[i] = tab[oy + r * SZ + i];
+              Z[i] = tab[oz + r * SZ + i];
+            }
+#pragma unroll
+            for (int e = 0; e < INNER; ++e)
+              v[e] += X[cart_e(LI, e, 0)] * Y[cart_e(LI, e, 1)] * Z[cart_e(LI, e, 2)];
+          }
+#pragma unroll
+          for (int e = 0; e < INNER; ++e) acc[j * INNER + e] += v[e];
+        }
       }
     }
     __syncwarp(gmask);
@@ -1043,7 +1083,7 @@ __device__ __forceinline__ void digest_grp(const KParams &kp, const QGeom<R> &g,
   __syncwarp(gmask);
 #pragma unroll
   for (int k = 0; k < Grp<LA, LB, LC, LD, R, T>::NPER; ++k) {
-    const int o = t + k * T;
+    const int o = Grp<LA, LB, LC, LD, R, T>::out(t, k);
     if (o < Q::NABCD) buf[o] = acc[k] * (R)Q::norm(o);
   }
   __syncwarp(gmask);
@@ -1274,7 +1314,7 @@ __global__ void __launch_bounds__(kBlock) eri_kernel(KParams kp, EriWork w) {
     if (p != 0) return;
 #pragma unroll
     for (int k = 0; k < GP::NPER; ++k) {
-      const int o = t + k * T;
+      const int o = GP::out(t, k);
       if (o < Q::NABCD)
         out[Q::ca(o) * s0 + Q::cb(o) * s1 + Q::cc(o) * s2 + Q::cd(o) * s3] = to_f64(acc[k] * (R)Q::norm(o));
     }
@@ -1307,7 +1347,7 @@ __global__ void __launch_bounds__(kBlock) schwarz_kernel(KParams kp, int p0, int
     eval_grp<LA, LB, LA, LB, R, T>(kp, g, buf, t, gmask, acc);
 #pragma unroll
     for (int k = 0; k < GP::NPER; ++k) {
-      const int o = t + k * T;
+      const int o = GP::out(t, k);
       if (o < Q::NABCD && Q::ca(o) == Q::cc(o) && Q::cb(o) == Q::cd(o))
         m = fmax(m, fabs((double)(acc[k] * (R)Q::norm(o))));
     }
