@@ -252,3 +252,79 @@ def test_profile_traffic_table_from_ncu_csv(tmp_path):
     assert table["jk_kernel<1,0,0,0,fp32>"][2:] == ["2", "1500"]
     assert abs(float(table["jk_kernel<2,2,2,2,fp64>"][1]) - 750.0 / 25) < 1e-4
     assert ("# csrc_sha16 " + PT.csrc_hash()) in out.read_text()
+
+
+ROWS_CHECK = r'''
+#include <cstdio>
+#include "classes.h"
+#include "quartet.cuh"
+using namespace sf;
+
+// lane t's k-th accumulator holds output (t + (k / INNER) T) INNER + k % INNER
+// (the mapping of Grp::out, a device function)
+template <int LA, int LB, int LC, int LD, typename R, int T>
+static int check_class() {
+  using Q = QC<LA, LB, LC, LD>;
+  using GP = Grp<LA, LB, LC, LD, R, T>;
+  int bad = 0;
+  static int seen[1296];
+  for (int o = 0; o < Q::NABCD; ++o) seen[o] = 0;
+  for (int t = 0; t < T; ++t)
+    for (int k = 0; k < GP::NPER; ++k) {
+      const int o = (t + (k / GP::INNER) * T) * GP::INNER + k % GP::INNER;
+      if (o < Q::NABCD) ++seen[o];
+    }
+  for (int o = 0; o < Q::NABCD; ++o) bad += seen[o] != 1;
+  if (GP::ROWS * GP::INNER != Q::NABCD || GP::RPER * T < GP::ROWS) ++bad;
+  if (GP::INNER > 1) {
+    for (int row = 0; row < GP::ROWS; ++row)
+      for (int e = 0; e < GP::INNER; ++e)
+        for (int d = 0; d < 3; ++d)
+          bad += Q::toff(row * GP::INNER + e, d) !=
+                 Q::toff(row * GP::INNER, d) - cart_e(GP::LI, 0, d) + cart_e(GP::LI, e, d);
+  }
+  if (2 * Q::NR * Q::SZ + Q::SZ >= 1024) ++bad;
+  printf("%d%d%d%d %s %d %d %d\n", LA, LB, LC, LD, sizeof(R) == 4 ? "fp32" : "fp64", GP::INNER, GP::NPER, bad);
+  return bad;
+}
+
+int main() {
+  int bad = 0;
+#define SF_CHK(id, la, lb, lc, ld, t64, t32)                     \
+  if (t32 > 1) bad += check_class<la, lb, lc, ld, float, t32>(); \
+  if (t64 > 1) bad += check_class<la, lb, lc, ld, double, t64>();
+  SF_CLASS_LIST(SF_CHK)
+#undef SF_CHK
+  return bad != 0;
+}
+'''
+
+
+def test_group_rows_cover_outputs_and_reuse_table_factors(tmp_path):
+    """The FP32 group kernels' row layout (quartet.cuh, Grp / eval_grp),
+    checked on the host against the library's own table offsets for every
+    class with more than one lane per quartet: the lanes' accumulators cover
+    each output exactly once; a row's outputs read 2-D factors that differ
+    only by the inner shell's exponent (consecutive entries); the packed
+    10-bit offsets fit; FP64 groups keep one output per row."""
+    import os
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc")
+    if nvcc is None and os.path.exists("/usr/local/cuda/bin/nvcc"):
+        nvcc = "/usr/local/cuda/bin/nvcc"
+    if nvcc is None:
+        pytest.skip("no nvcc")
+    src = tmp_path / "rows.cu"
+    src.write_text(ROWS_CHECK)
+    exe = tmp_path / "rows"
+    csrc = f"{REPO}/segfault_py_gb300/csrc"
+    subprocess.run([nvcc, "-std=c++17", "--expt-relaxed-constexpr", "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-I", f"{REPO}/include", "-I", csrc, str(src), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    rows = [l.split() for l in r.stdout.splitlines() if l.strip()]
+    assert r.returncode == 0, r.stdout
+    assert all(int(x[-1]) == 0 for x in rows)
+    inner = {(x[0], x[1]): int(x[2]) for x in rows}
+    assert inner[("2222", "fp32")] == 6 and inner[("2121", "fp32")] == 3 and inner[("2220", "fp32")] == 6
+    assert all(v == 1 for (k, p), v in inner.items() if p == "fp64")
